@@ -1,0 +1,619 @@
+// C ABI of libcontract.so: the contract.h drop-in entry points and the
+// contract_gb300.h extensions.  Validates arguments, builds the gamma
+// coefficient tables of each call, and hands the work to the kernel launchers.
+//
+// Error behaviour (CLQCD/contract lib/target/runtime_api_cuda.cpp:5-12 and the
+// launchers, e.g. lib/baryon/baryon.cu:43-45): an invalid selector prints a
+// message and exits with -1, a failed CUDA call exits with its error code.
+// That stays the default; contract_set_error_mode(CONTRACT_ERRORS_RECORD)
+// (or CONTRACT_ERROR_MODE=record) records the error and skips the call instead.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "contract_gb300.h"
+#include "gamma.hpp"
+#include "launch.hpp"
+
+namespace {
+
+using cgb::OpParams;
+
+std::mutex g_mu;
+int g_mode = -1;
+int g_err = CONTRACT_SUCCESS;
+std::string g_msg;
+cudaStream_t g_stream = nullptr;
+
+constexpr cgb::GammaTables kG = cgb::build_gamma_tables();
+
+struct DevState {
+  int num_sms = 0;
+  cgb::DeviceStatus *status = nullptr;
+  void *ws = nullptr;
+  size_t ws_bytes = 0;
+};
+DevState g_dev[64];
+
+int error_mode()
+{
+  if (g_mode < 0) {
+    const char *e = std::getenv("CONTRACT_ERROR_MODE");
+    g_mode = (e && std::strcmp(e, "record") == 0) ? CONTRACT_ERRORS_RECORD : CONTRACT_ERRORS_EXIT;
+  }
+  return g_mode;
+}
+
+// Report an error according to the error mode.  Always returns false.
+bool fail(int code, int exit_code, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (error_mode() == CONTRACT_ERRORS_EXIT) {
+    std::fprintf(stderr, "Error: %s\n", buf);
+    std::exit(exit_code);
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_err == CONTRACT_SUCCESS) {
+    g_err = code;
+    g_msg = buf;
+  }
+  return false;
+}
+
+bool invalid(const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  return fail(CONTRACT_ERROR_INVALID_ARGUMENT, -1, "%s", buf);
+}
+
+bool cuda_ok(cudaError_t e, const char *what)
+{
+  if (e == cudaSuccess) return true;
+  if (e == cudaErrorMemoryAllocation)
+    return fail(CONTRACT_ERROR_OUT_OF_MEMORY, (int)e, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+  return fail(CONTRACT_ERROR_CUDA, (int)e, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+}
+
+DevState *dev_state()
+{
+  int d = 0;
+  if (!cuda_ok(cudaGetDevice(&d), "cudaGetDevice")) return nullptr;
+  if (d < 0 || d >= 64) {
+    invalid("device ordinal %d out of range", d);
+    return nullptr;
+  }
+  DevState &s = g_dev[d];
+  if (s.num_sms == 0) {
+    int sms = 0;
+    if (!cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d), "cudaDeviceGetAttribute"))
+      return nullptr;
+    cgb::DeviceStatus *st = nullptr;
+    if (!cuda_ok(cgb::device_status_ptr(&st), "cudaGetSymbolAddress")) return nullptr;
+    s.status = st;
+    s.num_sms = sms;
+  }
+  return &s;
+}
+
+// Per-device scratch for per-timeslice partial sums; grows, never shrinks.
+struct DeviceWorkspace : cgb::Workspace {
+  DevState *s;
+  explicit DeviceWorkspace(DevState *st) : s(st) { }
+  void *get(size_t bytes) override
+  {
+    if (bytes <= s->ws_bytes) return s->ws;
+    size_t want = bytes > 2 * s->ws_bytes ? bytes : 2 * s->ws_bytes;
+    want = (want + 4095) & ~size_t(4095);
+    if (s->ws) {
+      // Kernels queued earlier may still read the old buffer.
+      if (cudaDeviceSynchronize() != cudaSuccess) return nullptr;
+      cudaFree(s->ws);
+      s->ws = nullptr;
+      s->ws_bytes = 0;
+    }
+    void *p = nullptr;
+    if (cudaMalloc(&p, want) != cudaSuccess) return nullptr;
+    s->ws = p;
+    s->ws_bytes = want;
+    return p;
+  }
+};
+
+bool gamma_ok(int g, const char *name)
+{
+  if (g >= 0 && g < 16) return true;
+  return invalid("Invalid %s value %d", name, g);
+}
+
+bool prec_ok(int p)
+{
+  if (p == CONTRACT_C128 || p == CONTRACT_C64) return true;
+  return invalid("Invalid precision value %d", p);
+}
+
+// Device buffers are moved with 16-byte bulk copies and 16-byte stores, so
+// every pointer must be 16-byte aligned (any complex128 array is; a complex64
+// view starting at an odd element is not).
+bool ptr_ok(const void *p, size_t volume, const char *name)
+{
+  if (volume == 0) return true;
+  if (p == nullptr) return invalid("%s is NULL", name);
+  if (reinterpret_cast<uintptr_t>(p) & 15u) return invalid("%s must be 16-byte aligned", name);
+  return true;
+}
+
+// Build the job: per-site (lattice == nullptr) or per-timeslice.  The
+// arguments are validated before any CUDA call is made.
+bool make_job(cgb::Job &job, int precision, size_t volume, const int *lattice, DevState **state = nullptr)
+{
+  job.per_site = lattice == nullptr;
+  if (lattice) {
+    const long long lx = lattice[0], ly = lattice[1], lz = lattice[2], lt = lattice[3];
+    if (lx <= 0 || ly <= 0 || lz <= 0 || lt <= 0 || (lx & 1))
+      return invalid("invalid lattice {%lld, %lld, %lld, %lld} (positive extents, Lx even)", lx, ly, lz, lt);
+    if (lx * ly * lz * lt != (long long)volume)
+      return invalid("volume %zu does not match lattice {%lld, %lld, %lld, %lld}", volume, lx, ly, lz, lt);
+    job.lt = (int)lt;
+    job.half_slice = lx * ly * lz / 2;
+  }
+  DevState *s = dev_state();
+  if (!s) return false;
+  job.prec = precision == CONTRACT_C64 ? cgb::Prec::C64 : cgb::Prec::C128;
+  job.stream = g_stream;
+  job.status = s->status;
+  job.num_sms = s->num_sms;
+  job.volume = (long long)volume;
+  if (state) *state = s;
+  return true;
+}
+
+void set_row(uint8_t dst[4], const uint8_t src[4])
+{
+  for (int k = 0; k < 4; ++k) dst[k] = src[k];
+}
+
+// Fill the projector operand from Gamma(gamma_mn) or a host 4x4 complex array.
+void fill_proj(cgb::ProjOperand<double> &w, int gamma_mn, const double *project_mn)
+{
+  w = {};
+  if (!project_mn) {
+    const cgb::SignedPerm g = cgb::sp_gamma(gamma_mn);
+    static const double re[4] = {1, 0, -1, 0}, im[4] = {0, 1, 0, -1};
+    for (int m = 0; m < 4; ++m) {
+      w.perm[m] = (uint8_t)g.perm[m];
+      w.ph[m] = (uint8_t)g.ph[m];
+      w.w[m * 4 + g.perm[m]][0] = re[g.ph[m]];
+      w.w[m * 4 + g.perm[m]][1] = im[g.ph[m]];
+    }
+    w.is_perm = 1;
+    return;
+  }
+  for (int k = 0; k < 16; ++k) {
+    w.w[k][0] = project_mn[2 * k];
+    w.w[k][1] = project_mn[2 * k + 1];
+  }
+  // A phased permutation (one entry in {1, i, -1, -i} per row, distinct
+  // columns) is applied with index/sign operations instead of multiplies.
+  bool perm = true;
+  int used = 0;
+  for (int m = 0; m < 4 && perm; ++m) {
+    int nz = 0, col = -1;
+    for (int n = 0; n < 4; ++n)
+      if (w.w[m * 4 + n][0] != 0.0 || w.w[m * 4 + n][1] != 0.0) {
+        ++nz;
+        col = n;
+      }
+    if (nz != 1 || (used >> col) & 1) {
+      perm = false;
+      break;
+    }
+    used |= 1 << col;
+    const double a = w.w[m * 4 + col][0], b = w.w[m * 4 + col][1];
+    int ph = -1;
+    if (a == 1.0 && b == 0.0) ph = 0;
+    else if (a == 0.0 && b == 1.0) ph = 1;
+    else if (a == -1.0 && b == 0.0) ph = 2;
+    else if (a == 0.0 && b == -1.0) ph = 3;
+    if (ph < 0) perm = false;
+    w.perm[m] = (uint8_t)col;
+    w.ph[m] = (uint8_t)(ph < 0 ? 0 : ph);
+  }
+  w.is_perm = perm ? 1 : 0;
+}
+
+// Contraction type -> canonical form (see ops.cuh): loop or triangle, whether
+// P_i and P_j swap roles, and the c1/c2 phase rows.
+struct TypeForm {
+  bool loop, swap_ij;
+  const uint8_t *c1, *c2;
+};
+
+TypeForm type_form(int type, int gij, int gkl)
+{
+  const bool sij = type == IM_JK_NL || type == IM_JL_NK;
+  const bool skl = type == IL_JK_NM || type == IL_JM_NK || type == IM_JL_NK;
+  TypeForm f;
+  f.loop = type == IK_JL_NM || type == IL_JK_NM;
+  f.swap_ij = sij;
+  f.c1 = sij ? kG.ph_t[gij] : kG.ph[gij];
+  f.c2 = skl ? kG.ph[gkl] : kG.ph_t[gkl];
+  return f;
+}
+
+bool type_ok(int type)
+{
+  if (type >= 0 && type < 6) return true;
+  return invalid("Invalid contract_type value %d", type);
+}
+
+void do_meson(void *correl, const void *pi, const void *pj, size_t volume, int gij, int gkl, int prec,
+              const int *lattice)
+{
+  if (!gamma_ok(gij, "gamma_ij") || !gamma_ok(gkl, "gamma_kl") || !prec_ok(prec)) return;
+  if (!ptr_ok(correl, volume, "correl") || !ptr_ok(pi, volume, "propag_i") || !ptr_ok(pj, volume, "propag_j")) return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, prec, volume, lattice, &s)) return;
+  DeviceWorkspace ws(s);
+  job.ws = &ws;
+  OpParams<double> p {};
+  p.in[0] = pi;
+  p.in[1] = pj;
+  p.out[0] = correl;
+  set_row(p.m.perm1, kG.perm[gij]);
+  set_row(p.m.ph1, kG.ph_g5g_t[gij]);
+  set_row(p.m.perm2, kG.perm[gkl]);
+  set_row(p.m.ph2, kG.ph_g5g_t[gkl]);
+  cuda_ok(cgb::launch_meson(job, p), "meson_two_point");
+}
+
+void do_meson_all(void **correl, const void *pi, const void *pj, size_t volume, int gamma, bool source, int prec,
+                  const int *lattice)
+{
+  if (!gamma_ok(gamma, source ? "gamma_ij" : "gamma_kl") || !prec_ok(prec)) return;
+  if (!correl) {
+    invalid("correl pointer array is NULL");
+    return;
+  }
+  for (int g = 0; g < 16; ++g)
+    if (!ptr_ok(correl[g], volume, "correl[g]")) return;
+  if (!ptr_ok(pi, volume, "propag_i") || !ptr_ok(pj, volume, "propag_j")) return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, prec, volume, lattice, &s)) return;
+  DeviceWorkspace ws(s);
+  job.ws = &ws;
+  OpParams<double> p {};
+  p.in[0] = pi;
+  p.in[1] = pj;
+  for (int g = 0; g < 16; ++g) p.out[g] = correl[g];
+  set_row(p.m.perm1, kG.perm[gamma]);
+  set_row(p.m.ph1, kG.ph_g5g_t[gamma]);
+  set_row(p.m.perm2, kG.perm[gamma]);
+  set_row(p.m.ph2, kG.ph_g5g_t[gamma]);
+  cuda_ok(cgb::launch_meson_all(job, source, p), source ? "meson_all_source_two_point" : "meson_all_sink_two_point");
+}
+
+void do_baryon(void *correl, const void *pi, const void *pj, const void *pn, int type, size_t volume, int gij, int gkl,
+               int gmn, const double *proj, int prec, const int *lattice)
+{
+  if (!type_ok(type)) return;
+  if (!proj && !gamma_ok(gmn, "gamma_mn")) return;
+  if (!gamma_ok(gij, "gamma_ij") || !gamma_ok(gkl, "gamma_kl") || !prec_ok(prec)) return;
+  if (!ptr_ok(correl, volume, "correl") || !ptr_ok(pi, volume, "propag_i") || !ptr_ok(pj, volume, "propag_j") ||
+      !ptr_ok(pn, volume, "propag_n"))
+    return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, prec, volume, lattice, &s)) return;
+  DeviceWorkspace ws(s);
+  job.ws = &ws;
+  const TypeForm f = type_form(type, gij, gkl);
+  OpParams<double> p {};
+  p.in[0] = f.swap_ij ? pj : pi;
+  p.in[1] = f.swap_ij ? pi : pj;
+  p.in[2] = pn;
+  p.out[0] = correl;
+  set_row(p.b.perm1, kG.perm[gij]);
+  set_row(p.b.perm2, kG.perm[gkl]);
+  set_row(p.b.ph1[0], f.c1);
+  set_row(p.b.ph2[0], f.c2);
+  fill_proj(p.b.proj[0], gmn, proj);
+  cuda_ok(cgb::launch_baryon(job, f.loop, p), proj ? "baryon_general_two_point" : "baryon_two_point");
+}
+
+void do_diquark(void *dq, const void *pi, const void *pj, size_t volume, int gij, int gkl, int prec)
+{
+  if (gij < 0 || gij >= 16) {
+    // The reference silently skips an unknown gamma_ij (lib/baryon/diquark.cu:40).
+    if (error_mode() == CONTRACT_ERRORS_RECORD) invalid("Invalid gamma_ij value %d", gij);
+    return;
+  }
+  if (!gamma_ok(gkl, "gamma_kl") || !prec_ok(prec)) return;
+  if (!ptr_ok(dq, volume, "diquark") || !ptr_ok(pi, volume, "propag_i") || !ptr_ok(pj, volume, "propag_j")) return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, prec, volume, nullptr, &s)) return;
+  OpParams<double> p {};
+  p.in[0] = pi;
+  p.in[1] = pj;
+  p.out[0] = dq;
+  set_row(p.b.perm1, kG.perm[gij]);
+  set_row(p.b.ph1[0], kG.ph[gij]);
+  set_row(p.b.perm2, kG.perm[gkl]);
+  set_row(p.b.ph2[0], kG.ph_t[gkl]);
+  cuda_ok(cgb::launch_diquark(job, p), "baryon_diquark");
+}
+
+void do_sequential(void *pi, void *pj, void *pn, int type, int seq, size_t volume, int gij, int gkl, int gmn, int prec)
+{
+  if (seq < 0 || seq > 2) {
+    // The reference silently skips an unknown sequential_type (lib/contract.cpp:60).
+    if (error_mode() == CONTRACT_ERRORS_RECORD) invalid("Invalid sequential_type value %d", seq);
+    return;
+  }
+  if (!type_ok(type) || !gamma_ok(gmn, "gamma_mn") || !gamma_ok(gij, "gamma_ij") || !gamma_ok(gkl, "gamma_kl") ||
+      !prec_ok(prec))
+    return;
+  if (!ptr_ok(pi, volume, "propag_i") || !ptr_ok(pj, volume, "propag_j") || !ptr_ok(pn, volume, "propag_n")) return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, prec, volume, nullptr, &s)) return;
+  const TypeForm f = type_form(type, gij, gkl);
+  const void *a = f.swap_ij ? pj : pi, *b = f.swap_ij ? pi : pj;
+  // Differentiated role: 0 = A, 1 = B, 2 = P_n.
+  const int role = seq == SEQUENTIAL_N ? 2 : (((seq == SEQUENTIAL_I) != f.swap_ij) ? 0 : 1);
+  OpParams<double> p {};
+  if (role == 0) {
+    p.in[0] = b;
+    p.in[1] = pn;
+  } else if (role == 1) {
+    p.in[0] = a;
+    p.in[1] = pn;
+  } else {
+    p.in[0] = a;
+    p.in[1] = b;
+  }
+  p.out[0] = seq == SEQUENTIAL_I ? pi : (seq == SEQUENTIAL_J ? pj : pn);
+  set_row(p.b.perm1, kG.perm[gij]);
+  set_row(p.b.perm2, kG.perm[gkl]);
+  set_row(p.b.ph1[0], f.c1);
+  set_row(p.b.ph2[0], f.c2);
+  fill_proj(p.b.proj[0], gmn, nullptr);
+  cuda_ok(cgb::launch_sequential(job, f.loop, role, p), "baryon_sequential_two_point");
+}
+
+} // namespace
+
+// Only the C ABI is exported (the library is built with -fvisibility=hidden).
+#pragma GCC visibility push(default)
+extern "C" {
+
+// ------------------------------------------------------------ contract.h --
+void init(int device) { cuda_ok(cudaSetDevice(device), "cudaSetDevice"); }
+
+void meson_two_point(void *correl, void *propag_i, void *propag_j, unsigned long volume, int gamma_ij, int gamma_kl)
+{
+  do_meson(correl, propag_i, propag_j, volume, gamma_ij, gamma_kl, CONTRACT_C128, nullptr);
+}
+
+void meson_all_source_two_point(void **correl, void *propag_i, void *propag_j, unsigned long volume, int gamma_ij)
+{
+  do_meson_all(correl, propag_i, propag_j, volume, gamma_ij, true, CONTRACT_C128, nullptr);
+}
+
+void meson_all_sink_two_point(void **correl, void *propag_i, void *propag_j, unsigned long volume, int gamma_kl)
+{
+  do_meson_all(correl, propag_i, propag_j, volume, gamma_kl, false, CONTRACT_C128, nullptr);
+}
+
+void baryon_diquark(void *diquark, void *propag_i, void *propag_j, size_t volume, int gamma_ij, int gamma_kl)
+{
+  do_diquark(diquark, propag_i, propag_j, volume, gamma_ij, gamma_kl, CONTRACT_C128);
+}
+
+void baryon_two_point(void *correl, void *propag_i, void *propag_j, void *propag_n, BaryonContractType contract_type,
+                      unsigned long volume, int gamma_ij, int gamma_kl, int gamma_mn)
+{
+  do_baryon(correl, propag_i, propag_j, propag_n, (int)contract_type, volume, gamma_ij, gamma_kl, gamma_mn, nullptr,
+            CONTRACT_C128, nullptr);
+}
+
+void baryon_general_two_point(void *correl, void *propag_i, void *propag_j, void *propag_n,
+                              BaryonContractType contract_type, size_t volume, int gamma_ij, int gamma_kl,
+                              void *project_mn)
+{
+  if (!project_mn) {
+    invalid("project_mn is NULL");
+    return;
+  }
+  do_baryon(correl, propag_i, propag_j, propag_n, (int)contract_type, volume, gamma_ij, gamma_kl, 0,
+            static_cast<const double *>(project_mn), CONTRACT_C128, nullptr);
+}
+
+void baryon_sequential_two_point(void *propag_i, void *propag_j, void *propag_n, BaryonContractType contract_type,
+                                 BaryonSequentialType sequential_type, size_t volume, int gamma_ij, int gamma_kl,
+                                 int gamma_mn)
+{
+  do_sequential(propag_i, propag_j, propag_n, (int)contract_type, (int)sequential_type, volume, gamma_ij, gamma_kl,
+                gamma_mn, CONTRACT_C128);
+}
+
+// ------------------------------------------------------ contract_gb300.h --
+void contract_set_error_mode(int mode)
+{
+  g_mode = mode == CONTRACT_ERRORS_RECORD ? CONTRACT_ERRORS_RECORD : CONTRACT_ERRORS_EXIT;
+}
+
+int contract_get_error_mode(void) { return error_mode(); }
+
+int contract_last_error(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_err;
+}
+
+const char *contract_last_error_message(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_msg.c_str();
+}
+
+void contract_clear_error(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_err = CONTRACT_SUCCESS;
+  g_msg.clear();
+}
+
+int contract_check_device(void)
+{
+  DevState *s = dev_state();
+  if (!s) return contract_last_error();
+  if (!cuda_ok(cudaStreamSynchronize(g_stream), "cudaStreamSynchronize")) return contract_last_error();
+  cgb::DeviceStatus st {};
+  if (!cuda_ok(cudaMemcpy(&st, s->status, sizeof(st), cudaMemcpyDeviceToHost), "status readback"))
+    return contract_last_error();
+  if (st.flags) {
+    const cgb::DeviceStatus zero {};
+    cudaMemcpy(s->status, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+    if (st.flags & cgb::kDevErrWaitTimeout)
+      fail(CONTRACT_ERROR_DEVICE_TIMEOUT, -1, "a kernel timed out waiting for its copies (chunk %u)", st.where);
+    else
+      fail(CONTRACT_ERROR_BAD_WORK, -1, "a work descriptor failed validation (item %u)", st.where);
+  }
+  return contract_last_error();
+}
+
+void contract_set_stream(void *stream) { g_stream = static_cast<cudaStream_t>(stream); }
+
+void *contract_get_stream(void) { return g_stream; }
+
+size_t contract_workspace_bytes(const int *lattice, int noutputs)
+{
+  if (!lattice || noutputs <= 0) return 0;
+  const long long half = (long long)lattice[0] * lattice[1] * lattice[2] / 2;
+  // Upper bound over the tile shapes in use (smallest tile: 8 sites, one
+  // partial per chunk of at least one tile).
+  const long long tiles = (half + 7) / 8 * 2 * lattice[3];
+  return (size_t)tiles * noutputs * 16;
+}
+
+int contract_workspace_reserve(size_t bytes)
+{
+  DevState *s = dev_state();
+  if (!s) return contract_last_error();
+  DeviceWorkspace ws(s);
+  if (!ws.get(bytes)) {
+    fail(CONTRACT_ERROR_OUT_OF_MEMORY, (int)cudaErrorMemoryAllocation, "workspace of %zu bytes", bytes);
+    return contract_last_error();
+  }
+  return CONTRACT_SUCCESS;
+}
+
+void contract_gamma_table(int *perm, int *phase)
+{
+  for (int n = 0; n < 16; ++n)
+    for (int r = 0; r < 4; ++r) {
+      if (perm) perm[n * 4 + r] = kG.perm[n][r];
+      if (phase) phase[n * 4 + r] = kG.ph[n][r];
+    }
+}
+
+void contract_convert_precision(void *dst, const void *src, size_t volume, int to_c64)
+{
+  if (!ptr_ok(dst, volume, "dst") || !ptr_ok(src, volume, "src")) return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, CONTRACT_C128, volume, nullptr, &s)) return;
+  cuda_ok(cgb::launch_convert(job, dst, src, to_c64 != 0), "contract_convert_precision");
+}
+
+void contract_meson(void *correl, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
+                    int gamma_kl, int precision, const int *lattice)
+{
+  do_meson(correl, propag_i, propag_j, volume, gamma_ij, gamma_kl, precision, lattice);
+}
+
+void contract_meson_all(void **correl, const void *propag_i, const void *propag_j, size_t volume, int fixed_gamma,
+                        int source, int precision, const int *lattice)
+{
+  do_meson_all(correl, propag_i, propag_j, volume, fixed_gamma, source != 0, precision, lattice);
+}
+
+void contract_baryon(void *correl, const void *propag_i, const void *propag_j, const void *propag_n,
+                     BaryonContractType contract_type, size_t volume, int gamma_ij, int gamma_kl, int gamma_mn,
+                     const void *project_mn, int precision, const int *lattice)
+{
+  do_baryon(correl, propag_i, propag_j, propag_n, (int)contract_type, volume, gamma_ij, gamma_kl, gamma_mn,
+            static_cast<const double *>(project_mn), precision, lattice);
+}
+
+void contract_baryon_all_types(void *correl, const void *propag_i, const void *propag_j, const void *propag_n,
+                               size_t volume, int gamma_ij, int gamma_kl, int nproj, const void *projectors,
+                               int precision, const int *lattice)
+{
+  if (nproj < 1 || nproj > 2) {
+    invalid("nproj must be 1 or 2 (got %d)", nproj);
+    return;
+  }
+  if (!projectors) {
+    invalid("projectors is NULL");
+    return;
+  }
+  if (!gamma_ok(gamma_ij, "gamma_ij") || !gamma_ok(gamma_kl, "gamma_kl") || !prec_ok(precision)) return;
+  if (!ptr_ok(correl, volume, "correl") || !ptr_ok(propag_i, volume, "propag_i") ||
+      !ptr_ok(propag_j, volume, "propag_j") || !ptr_ok(propag_n, volume, "propag_n"))
+    return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, precision, volume, lattice, &s)) return;
+  DeviceWorkspace ws(s);
+  job.ws = &ws;
+  OpParams<double> p {};
+  p.in[0] = propag_i;
+  p.in[1] = propag_j;
+  p.in[2] = propag_n;
+  const size_t stride = lattice ? (size_t)lattice[3] : volume;
+  for (int o = 0; o < 6 * nproj; ++o) p.out[o] = static_cast<char *>(correl) + o * stride * 16;
+  set_row(p.b.perm1, kG.perm[gamma_ij]);
+  set_row(p.b.perm2, kG.perm[gamma_kl]);
+  set_row(p.b.ph1[0], kG.ph[gamma_ij]);    // A = P_i groups
+  set_row(p.b.ph1[1], kG.ph_t[gamma_ij]);  // IM_* group (A = P_j)
+  set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);  // IK_JL_NM, IK_JM_NL, IM_JK_NL
+  set_row(p.b.ph2[1], kG.ph[gamma_kl]);    // IL_JK_NM, IL_JM_NK, IM_JL_NK
+  const double *pr = static_cast<const double *>(projectors);
+  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pr + 32 * w);
+  cuda_ok(cgb::launch_baryon_fused(job, nproj, p), "contract_baryon_all_types");
+}
+
+void contract_diquark(void *diquark, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
+                      int gamma_kl, int precision)
+{
+  do_diquark(diquark, propag_i, propag_j, volume, gamma_ij, gamma_kl, precision);
+}
+
+void contract_sequential(void *propag_i, void *propag_j, void *propag_n, BaryonContractType contract_type,
+                         BaryonSequentialType sequential_type, size_t volume, int gamma_ij, int gamma_kl,
+                         int gamma_mn, int precision)
+{
+  do_sequential(propag_i, propag_j, propag_n, (int)contract_type, (int)sequential_type, volume, gamma_ij, gamma_kl,
+                gamma_mn, precision);
+}
+
+} // extern "C"
+#pragma GCC visibility pop

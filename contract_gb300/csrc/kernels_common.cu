@@ -1,0 +1,57 @@
+// Per-timeslice finalisation and precision conversion kernels.
+#include "launch_impl.cuh"
+
+namespace cgb {
+
+__device__ DeviceStatus g_device_status;
+
+cudaError_t device_status_ptr(DeviceStatus **out) { return cudaGetSymbolAddress((void **)out, g_device_status); }
+
+// out.p[o][t] = sum_{parity, chunk} partial[((parity*lt + t)*chunks_per_seg + chunk)*nout + o]
+// Segments are half-timeslices in PyQUDA order [parity][t][...]; the sum runs
+// in FP64 in a fixed order, so results are bitwise reproducible.
+__global__ void finalize_kernel(const double2 *__restrict__ partial, OutPtrs out, int nout, int lt, int chunks_per_seg)
+{
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nout * lt) return;
+  const int o = idx / lt, t = idx % lt;
+  double sx = 0.0, sy = 0.0;
+  for (int par = 0; par < 2; ++par) {
+    const double2 *row = partial + ((size_t)(par * lt + t) * chunks_per_seg) * nout + o;
+    for (int c = 0; c < chunks_per_seg; ++c) {
+      const double2 v = row[(size_t)c * nout];
+      sx += v.x;
+      sy += v.y;
+    }
+  }
+  out.p[o][t] = make_double2(sx, sy);
+}
+
+// complex128 <-> complex64, one complex per thread step, grid-stride.
+__global__ void c128_to_c64(float2 *__restrict__ dst, const double2 *__restrict__ src, long long n)
+{
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const double2 v = src[k];
+    dst[k] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+__global__ void c64_to_c128(double2 *__restrict__ dst, const float2 *__restrict__ src, long long n)
+{
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const float2 v = src[k];
+    dst[k] = make_double2((double)v.x, (double)v.y);
+  }
+}
+
+cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64)
+{
+  const long long n = job.volume * 144;
+  if (n == 0) return cudaSuccess;
+  const int grid = job.num_sms * 8;
+  if (to_c64) c128_to_c64<<<grid, 256, 0, job.stream>>>(static_cast<float2 *>(dst), static_cast<const double2 *>(src), n);
+  else c64_to_c128<<<grid, 256, 0, job.stream>>>(static_cast<double2 *>(dst), static_cast<const float2 *>(src), n);
+  return cudaGetLastError();
+}
+
+} // namespace cgb

@@ -1,0 +1,82 @@
+// Internal host interface between the C ABI (abi.cpp) and the kernel
+// translation units.  Not part of the public headers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "ops.cuh"
+
+namespace cgb {
+
+enum class Prec { C128 = 0, C64 = 1 };
+
+// Device scratch provider (partial sums of the per-timeslice reductions).
+struct Workspace {
+  virtual ~Workspace() = default;
+  // Returns a device buffer of at least `bytes`, or nullptr on failure.
+  virtual void *get(size_t bytes) = 0;
+};
+
+struct Job {
+  Prec prec = Prec::C128;
+  cudaStream_t stream = 0;
+  DeviceStatus *status = nullptr;
+  int num_sms = 1;
+  long long volume = 0;
+  // Per-site outputs (the reference's semantics) or per-timeslice sums.
+  bool per_site = true;
+  int lt = 0;                // timeslices (per_site == false)
+  long long half_slice = 0;  // sites per (parity, t) segment = Lx*Ly*Lz/2
+  Workspace *ws = nullptr;
+};
+
+// Every launcher fills the geometry for its own tile shape and returns the
+// CUDA error of the launch (cudaSuccess when volume == 0).
+cudaError_t launch_meson(const Job &job, const OpParams<double> &p);
+cudaError_t launch_meson_all(const Job &job, bool source, const OpParams<double> &p);
+cudaError_t launch_baryon(const Job &job, bool loop, const OpParams<double> &p);
+cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &p);
+cudaError_t launch_diquark(const Job &job, const OpParams<double> &p);
+cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParams<double> &p);
+cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64);
+// Address of this device's status word (a __device__ variable of the library).
+cudaError_t device_status_ptr(DeviceStatus **out);
+
+// ---- helpers shared by the launcher TUs --------------------------------------
+template <class R> OpParams<R> convert_params(const OpParams<double> &p)
+{
+  OpParams<R> o {};
+  for (int k = 0; k < 3; ++k) o.in[k] = p.in[k];
+  for (int k = 0; k < 16; ++k) o.out[k] = p.out[k];
+  o.geom = p.geom;
+  o.status = p.status;
+  for (int k = 0; k < 4; ++k) {
+    o.b.perm1[k] = p.b.perm1[k];
+    o.b.perm2[k] = p.b.perm2[k];
+    o.m.perm1[k] = p.m.perm1[k];
+    o.m.perm2[k] = p.m.perm2[k];
+    o.m.ph1[k] = p.m.ph1[k];
+    o.m.ph2[k] = p.m.ph2[k];
+    for (int v = 0; v < 2; ++v) {
+      o.b.ph1[v][k] = p.b.ph1[v][k];
+      o.b.ph2[v][k] = p.b.ph2[v][k];
+    }
+  }
+  for (int w = 0; w < 2; ++w) {
+    const ProjOperand<double> &s = p.b.proj[w];
+    ProjOperand<R> &d = o.b.proj[w];
+    for (int k = 0; k < 16; ++k) {
+      d.w[k][0] = R(s.w[k][0]);
+      d.w[k][1] = R(s.w[k][1]);
+    }
+    for (int k = 0; k < 4; ++k) {
+      d.perm[k] = s.perm[k];
+      d.ph[k] = s.ph[k];
+    }
+    d.is_perm = s.is_perm;
+  }
+  return o;
+}
+
+} // namespace cgb

@@ -1,0 +1,556 @@
+// Per-site contraction routines and the kernel "ops" that plug them into the
+// tile engines (engine.cuh).
+//
+// Notation (one lattice site): a propagator P[s0][s1][c0][c1] is 16 colour
+// blocks of 9 complex numbers; block (s0, s1) starts at (4*s0 + s1)*9.
+// Gamma coefficients are phase codes (powers of i) and permutations:
+//   c1(i) on spin row i with partner j = perm1[i]   (from Gamma_ij)
+//   c2(l) on spin column l with partner k = perm2[l] (from Gamma_kl)
+//
+// Baryon two-point, canonical forms (F = eps.eps trilinear form, X ^ Y the
+// colour wedge of common.cuh, W the 4x4 Gamma_mn/projector operand):
+//   loop     C = sum_{i,l} c1(i) c2(l) F(A[i][perm2 l], B[perm1 i][l], Q),
+//            Q = sum_{m,n} W[m][n] N[n][m]
+//   triangle C = sum_{i,l} c1(i) c2(l) A[i][perm2 l] . sum_m (B[perm1 i][m] ^ N'[m][l]),
+//            N'[m][l] = sum_n W[m][n] N[n][l]
+// The six contract_enum.h types map onto these (CLQCD/contract
+// include/baryon.cuh:43-83, baryon_general.cuh:45-93):
+//   IK_JL_NM loop (A=P_i, B=P_j, c1 = Gamma_ij,   c2 = Gamma_kl^T)
+//   IL_JK_NM loop (A=P_i, B=P_j, c1 = Gamma_ij,   c2 = Gamma_kl)
+//   IK_JM_NL tri  (A=P_i, B=P_j, c1 = Gamma_ij,   c2 = Gamma_kl^T)
+//   IL_JM_NK tri  (A=P_i, B=P_j, c1 = Gamma_ij,   c2 = Gamma_kl)
+//   IM_JK_NL tri  (A=P_j, B=P_i, c1 = Gamma_ij^T, c2 = Gamma_kl^T)
+//   IM_JL_NK tri  (A=P_j, B=P_i, c1 = Gamma_ij^T, c2 = Gamma_kl)
+// Types that differ only in c2 share every wedge, which the fused kernel
+// exploits: IK_JL/IL_JK, IK_JM/IL_JM and IM_JK/IM_JL each cost one evaluation.
+//
+// Thread mapping: TPS threads per site; thread `sub` owns spin row
+// i = sub / (TPS/4) and LPT = 16/TPS consecutive columns l.
+#pragma once
+
+#include "engine.cuh"
+#include "gamma.hpp"
+
+namespace cgb {
+
+// Projector operand W[m][n] (the Gamma_mn slot).  When W is a phased
+// permutation (always true for a Gamma matrix) the kernels use perm/ph and
+// do no multiplications with it.
+template <class R> struct ProjOperand {
+  R w[16][2];
+  uint8_t perm[4];
+  uint8_t ph[4];
+  int is_perm;
+};
+
+template <class R> struct BaryonSpin {
+  uint8_t perm1[4], perm2[4];
+  uint8_t ph1[2][4];  // [0]: c1 for A = P_i groups, [1]: c1 for the swapped (IM_*) group
+  uint8_t ph2[2][4];  // c2 variants (one per output of a loop/tri evaluation)
+  ProjOperand<R> proj[2];
+};
+
+template <class R> struct MesonSpin {
+  uint8_t perm1[4], perm2[4];
+  uint8_t ph1[4], ph2[4];
+};
+
+template <class R> struct OpParams {
+  const void *in[3];
+  void *out[16];
+  TileGeom geom;
+  DeviceStatus *status;
+  BaryonSpin<R> b;
+  MesonSpin<R> m;
+};
+
+template <int TPS> struct Lanes {
+  static constexpr int TPI = TPS / 4;  // threads per spin row
+  static constexpr int LPT = 4 / TPI;  // spin columns per thread
+  static_assert(TPS == 4 || TPS == 8 || TPS == 16, "TPS must be 4, 8 or 16");
+};
+
+template <class R> __device__ __forceinline__ bool nonzero(const R w[2]) { return w[0] != R(0) || w[1] != R(0); }
+
+// Q_w[ad] = sum_{m,n} W[m][n] N[n][m][ad], one entry per thread, into smem q[w*9 + ad].
+template <class R, class S, int TPS, int NW>
+__device__ __forceinline__ void build_q(const BaryonSpin<R> &b, const S *N, S *q, int sub)
+{
+  for (int e = sub; e < 9 * NW; e += TPS) {
+    const int w = e / 9, ad = e % 9;
+    const ProjOperand<R> &pw = b.proj[w];
+    cx<R> s = czero<R>();
+    if (pw.is_perm) {
+#pragma unroll
+      for (int m = 0; m < 4; ++m) s = cadd(s, mul_phase(ld<R>(N + (pw.perm[m] * 4 + m) * 9 + ad), pw.ph[m]));
+    } else {
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+          if (nonzero(pw.w[m * 4 + n])) cfma(s, cx<R> {pw.w[m * 4 + n][0], pw.w[m * 4 + n][1]}, ld<R>(N + (n * 4 + m) * 9 + ad));
+    }
+    st(q + e, s);
+  }
+}
+
+// N'_w[m][l] = sum_n W[m][n] N[n][l] into the w-th scratch slot.
+template <class R, class S, int TPS, int NW>
+__device__ __forceinline__ void build_nprime(const BaryonSpin<R> &b, const S *N, S *np, int sub)
+{
+  for (int e = sub; e < 16 * NW; e += TPS) {
+    const int w = e / 16, blk = e % 16, m = blk / 4, l = blk % 4;
+    const ProjOperand<R> &pw = b.proj[w];
+    S *dst = np + (size_t)w * 144 + blk * 9;
+    if (pw.is_perm) {
+      const S *src = N + (pw.perm[m] * 4 + l) * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) st(dst + k, mul_phase(ld<R>(src + k), pw.ph[m]));
+    } else {
+      cx<R> o[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) o[k] = czero<R>();
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        if (!nonzero(pw.w[m * 4 + n])) continue;
+        const cx<R> wv {pw.w[m * 4 + n][0], pw.w[m * 4 + n][1]};
+#pragma unroll
+        for (int k = 0; k < 9; ++k) cfma(o[k], wv, ld<R>(N + (n * 4 + l) * 9 + k));
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) st(dst + k, o[k]);
+    }
+  }
+}
+
+// Loop form.  Writes vals[v*NW + w] (partial over this thread's (i, l) pairs).
+template <class R, class S, int TPS, int NV, int NW>
+__device__ __forceinline__ void loop_site(const BaryonSpin<R> &b, const S *A, const S *B, const S *q, int sub, int c1sel,
+                                          cx<R> *vals)
+{
+  using Ln = Lanes<TPS>;
+  const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT;
+  const int j = b.perm1[i];
+  cx<R> r[NV][9];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) r[v][k] = czero<R>();
+#pragma unroll
+  for (int lo = 0; lo < Ln::LPT; ++lo) {
+    const int l = l0 + lo;
+    cx<R> x[9], y[9];
+    load9(x, A + (i * 4 + b.perm2[l]) * 9);
+    load9(y, B + (j * 4 + l) * 9);
+    if constexpr (NV == 1) {
+      phase9(x, b.ph2[0][l]);
+      wedge_acc(r[0], x, y);
+    } else {
+      cx<R> t[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) t[k] = czero<R>();
+      wedge_acc(t, x, y);
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) r[v][k] = cadd(r[v][k], mul_phase(t[k], b.ph2[v][l]));
+    }
+  }
+  const uint32_t p1 = b.ph1[c1sel][i];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    cx<R> qw[9];
+    load9(qw, q + w * 9);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) vals[v * NW + w] = mul_phase(dot9(r[v], qw), p1);
+  }
+}
+
+// Triangle form over N' (NW slots of 144 complex).  Writes vals[v*NW + w].
+template <class R, class S, int TPS, int NV, int NW>
+__device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A, const S *B, const S *np, int sub,
+                                              int c1sel, cx<R> *vals)
+{
+  using Ln = Lanes<TPS>;
+  const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT;
+  const int j = b.perm1[i];
+  cx<R> acc[NV][NW];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int w = 0; w < NW; ++w) acc[v][w] = czero<R>();
+
+  constexpr bool kCacheB = Ln::LPT > 1;
+  cx<R> brow[kCacheB ? 4 : 1][9];
+  if constexpr (kCacheB) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) load9(brow[m], B + (j * 4 + m) * 9);
+  }
+#pragma unroll
+  for (int lo = 0; lo < Ln::LPT; ++lo) {
+    const int l = l0 + lo;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      cx<R> d[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) d[k] = czero<R>();
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        cx<R> nn[9];
+        load9(nn, np + (size_t)w * 144 + (m * 4 + l) * 9);
+        if constexpr (kCacheB) {
+          wedge_acc(d, brow[m], nn);
+        } else {
+          cx<R> bm[9];
+          load9(bm, B + (j * 4 + m) * 9);
+          wedge_acc(d, bm, nn);
+        }
+      }
+      cx<R> a[9];
+      load9(a, A + (i * 4 + b.perm2[l]) * 9);
+      const cx<R> s = dot9(a, d);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(s, b.ph2[v][l]));
+    }
+  }
+  const uint32_t p1 = b.ph1[c1sel][i];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int w = 0; w < NW; ++w) vals[v * NW + w] = mul_phase(acc[v][w], p1);
+}
+
+// ------------------------------------------------------------------ ops --
+// Common compile-time configuration of an op.
+template <class R_, class S_, int SITES_, int TPS_, int NST_> struct OpBase {
+  using R = R_;
+  using S = S_;
+  using Params = OpParams<R_>;
+  static constexpr int SITES = SITES_, TPS = TPS_, NST = NST_;
+  static constexpr int THREADS = SITES_ * TPS_;
+  static_assert(32 % TPS_ == 0, "a site's threads must sit in one warp");
+};
+
+// One baryon contraction type per launch, loop form (IK_JL_NM, IL_JK_NM).
+template <class R, class S, int SITES, int TPS, int NST>
+struct BaryonLoopOp : OpBase<R, S, SITES, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 1, EXTRA_SLOTS = 1;
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    build_q<R, S, TPS, 1>(p.b, in[2], scratch, sub);
+    __syncwarp();
+    loop_site<R, S, TPS, 1, 1>(p.b, in[0], in[1], scratch, sub, 0, vals);
+  }
+};
+
+// One baryon contraction type per launch, triangle form (the other four types).
+template <class R, class S, int SITES, int TPS, int NST>
+struct BaryonTriOp : OpBase<R, S, SITES, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 1, EXTRA_SLOTS = 1;
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    build_nprime<R, S, TPS, 1>(p.b, in[2], scratch, sub);
+    __syncwarp();
+    triangle_site<R, S, TPS, 1, 1>(p.b, in[0], in[1], scratch, sub, 0, vals);
+  }
+};
+
+// All six types x NW projectors in one pass over (P_i, P_j, P_n).
+// Output o = type * NW + w, types in contract_enum.h order.
+template <class R, class S, int SITES, int TPS, int NST, int NW>
+struct BaryonFusedOp : OpBase<R, S, SITES, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_SLOTS = NW + 1;
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    S *q = scratch + (size_t)NW * 144;
+    build_nprime<R, S, TPS, NW>(p.b, in[2], scratch, sub);
+    build_q<R, S, TPS, NW>(p.b, in[2], q, sub);
+    __syncwarp();
+    cx<R> t[2 * NW];
+    loop_site<R, S, TPS, 2, NW>(p.b, in[0], in[1], q, sub, 0, t);  // IK_JL_NM, IL_JK_NM
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      vals[0 * NW + w] = t[0 * NW + w];
+      vals[2 * NW + w] = t[1 * NW + w];
+    }
+    triangle_site<R, S, TPS, 2, NW>(p.b, in[0], in[1], scratch, sub, 0, t);  // IK_JM_NL, IL_JM_NK
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      vals[1 * NW + w] = t[0 * NW + w];
+      vals[3 * NW + w] = t[1 * NW + w];
+    }
+    triangle_site<R, S, TPS, 2, NW>(p.b, in[1], in[0], scratch, sub, 1, t);  // IM_JK_NL, IM_JL_NK
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      vals[4 * NW + w] = t[0 * NW + w];
+      vals[5 * NW + w] = t[1 * NW + w];
+    }
+  }
+};
+
+// Meson two-point: C = sum_{i,l} c1(i) c2(l) sum_ad A[i][perm2 l][ad] conj(B[perm1 i][l][ad])
+// with c from (g5 Gamma)^T (include/meson.cuh:33-50).
+template <class R, class S, int SITES, int TPS, int NST>
+struct MesonOp : OpBase<R, S, SITES, TPS, NST> {
+  static constexpr int NIN = 2, NOUT = 1, EXTRA_SLOTS = 0;
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
+  {
+    using Ln = Lanes<TPS>;
+    const MesonSpin<R> &m = p.m;
+    const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT;
+    const int j = m.perm1[i];
+    cx<R> acc = czero<R>();
+#pragma unroll
+    for (int lo = 0; lo < Ln::LPT; ++lo) {
+      const int l = l0 + lo;
+      const S *x = in[0] + (i * 4 + m.perm2[l]) * 9;
+      const S *y = in[1] + (j * 4 + l) * 9;
+      cx<R> t = czero<R>();
+#pragma unroll
+      for (int k = 0; k < 9; ++k) cfma_conj(t, ld<R>(x + k), ld<R>(y + k));
+      acc = cadd(acc, mul_phase(t, m.ph2[l]));
+    }
+    vals[0] = mul_phase(acc, m.ph1[i]);
+  }
+};
+
+template <class R> __device__ __forceinline__ cx<R> pick4(const cx<R> t[4], int k)
+{
+  return k == 0 ? t[0] : (k == 1 ? t[1] : (k == 2 ? t[2] : t[3]));
+}
+
+// meson_all_source_two_point: Gamma_ij fixed (perm1/ph1), all 16 Gamma_kl.
+// Thread = spin row i (TPS = 4); the 4 x 4 colour dots T[k][l] for j = perm1[i]
+// are shared by all 16 outputs (include/meson_all.cuh:53-73 recomputes them per Gamma).
+template <class R, class S, int SITES, int NST>
+struct MesonAllSourceOp : OpBase<R, S, SITES, 4, NST> {
+  static constexpr int NIN = 2, NOUT = 16, EXTRA_SLOTS = 0;
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
+  {
+    constexpr GammaTables G = build_gamma_tables();
+    const int i = sub, j = p.m.perm1[i];
+#pragma unroll
+    for (int g = 0; g < 16; ++g) vals[g] = czero<R>();
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      cx<R> t[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        t[k] = czero<R>();
+        const S *x = in[0] + (i * 4 + k) * 9;
+        const S *y = in[1] + (j * 4 + l) * 9;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) cfma_conj(t[k], ld<R>(x + e), ld<R>(y + e));
+      }
+#pragma unroll
+      for (int g = 0; g < 16; ++g) vals[g] = cadd(vals[g], mul_phase(pick4(t, G.perm[g][l]), G.ph_g5g_t[g][l]));
+    }
+    const uint32_t p1 = p.m.ph1[i];
+#pragma unroll
+    for (int g = 0; g < 16; ++g) vals[g] = mul_phase(vals[g], p1);
+  }
+};
+
+// meson_all_sink_two_point: Gamma_kl fixed (perm2/ph2), all 16 Gamma_ij.
+// Thread = spin column l (TPS = 4).
+template <class R, class S, int SITES, int NST>
+struct MesonAllSinkOp : OpBase<R, S, SITES, 4, NST> {
+  static constexpr int NIN = 2, NOUT = 16, EXTRA_SLOTS = 0;
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
+  {
+    constexpr GammaTables G = build_gamma_tables();
+    const int l = sub, k = p.m.perm2[l];
+#pragma unroll
+    for (int g = 0; g < 16; ++g) vals[g] = czero<R>();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      cx<R> t[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        t[j] = czero<R>();
+        const S *x = in[0] + (i * 4 + k) * 9;
+        const S *y = in[1] + (j * 4 + l) * 9;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) cfma_conj(t[j], ld<R>(x + e), ld<R>(y + e));
+      }
+#pragma unroll
+      for (int g = 0; g < 16; ++g) vals[g] = cadd(vals[g], mul_phase(pick4(t, G.perm[g][i]), G.ph_g5g_t[g][i]));
+    }
+    const uint32_t p2 = p.m.ph2[l];
+#pragma unroll
+    for (int g = 0; g < 16; ++g) vals[g] = mul_phase(vals[g], p2);
+  }
+};
+
+// ----------------------------------------------------------- field ops --
+// Diquark (include/diquark.cuh:33-57):
+//   D[m][l][ad] = g5[m] g5[l] conj( c2(l) sum_i c1(i) (P_i[i][perm2 l] ^ P_j[perm1 i][m])[ad] )
+// with c1 from Gamma_ij, c2 from Gamma_kl^T.  Thread handles 16/TPS blocks (m, l).
+template <class R, class S, int SITES, int TPS, int NST>
+struct DiquarkOp : OpBase<R, S, SITES, TPS, NST> {
+  static constexpr int NIN = 2, EXTRA_SLOTS = 0;
+  static constexpr bool FIELD = true;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)
+  {
+    const BaryonSpin<R> &b = p.b;
+    for (int blk = sub; blk < 16; blk += TPS) {
+      const int m = blk / 4, l = blk % 4, k = b.perm2[l];
+      cx<R> d[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) d[e] = czero<R>();
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        cx<R> x[9], y[9];
+        load9(x, in[0] + (i * 4 + k) * 9);
+        load9(y, in[1] + (b.perm1[i] * 4 + m) * 9);
+        phase9(x, b.ph1[0][i]);
+        wedge_acc(d, x, y);
+      }
+      // g5[m] g5[l] = -1 when exactly one of m, l is a lower spin component.
+      const uint32_t sgn = ((m >> 1) ^ (l >> 1)) & 1u;
+      const uint32_t p2 = b.ph2[0][l];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        cx<R> v = conj(mul_phase(d[e], p2));
+        v.x = flip_sign(v.x, sgn);
+        v.y = flip_sign(v.y, sgn);
+        st(out + blk * 9 + e, v);
+      }
+    }
+  }
+};
+
+// Sequential source: the slot's propagator is overwritten with dC/dP_slot
+// (include/baryon_sequential.cuh:36-163).  With the canonical forms above,
+// A/B/N denote the roles; `role` is which one is differentiated.  Inputs are
+// the two other roles in (A, B, N) order.  W is always a Gamma matrix here.
+//   loop, d/dA[i][perm2 l] = c1 c2 (B[perm1 i][l] ^ Q)
+//   loop, d/dB[perm1 i][l] = c1 c2 (A[i][perm2 l] ^ Q)
+//   loop, d/dN[perm(m)][m] = W[m][perm m] * sum_{i,l} c1 c2 (A ^ B)
+//   tri,  d/dA[i][perm2 l] = c1 c2 sum_m B[perm1 i][m] ^ N'[m][l]
+//   tri,  d/dB[perm1 i][m] = c1 sum_l c2 (A[i][perm2 l] ^ N'[m][l])
+//   tri,  d/dN[perm(m)][l] = W[m][perm m] sum_i c1 c2 (A[i][perm2 l] ^ B[perm1 i][m])
+template <class R, class S, int SITES, int TPS, int NST, bool LOOP, int ROLE>
+struct SequentialOp : OpBase<R, S, SITES, TPS, NST> {
+  static constexpr int NIN = 2, EXTRA_SLOTS = 1;
+  static constexpr bool FIELD = true;
+
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, S *out)
+  {
+    const BaryonSpin<R> &b = p.b;
+    const ProjOperand<R> &pw = b.proj[0];
+    const S *A = ROLE == 0 ? nullptr : in[0];
+    const S *B = ROLE == 1 ? nullptr : (ROLE == 0 ? in[0] : in[1]);
+    const S *N = ROLE == 2 ? nullptr : in[1];
+    if constexpr (LOOP && ROLE != 2) {
+      build_q<R, S, TPS, 1>(b, N, scratch, sub);
+      __syncwarp();
+    }
+    if constexpr (!LOOP && ROLE != 2) {
+      build_nprime<R, S, TPS, 1>(b, N, scratch, sub);
+      __syncwarp();
+    }
+    if constexpr (LOOP && ROLE == 2) {
+      // R = sum_{i,l} c1 c2 (A ^ B): each thread its (i, l) share, then a group sum.
+      using Ln = Lanes<TPS>;
+      const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT, j = b.perm1[i];
+      cx<R> r[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) r[e] = czero<R>();
+#pragma unroll
+      for (int lo = 0; lo < Ln::LPT; ++lo) {
+        const int l = l0 + lo;
+        cx<R> x[9], y[9];
+        load9(x, A + (i * 4 + b.perm2[l]) * 9);
+        load9(y, B + (j * 4 + l) * 9);
+        phase9(x, (b.ph1[0][i] + b.ph2[0][l]) & 3u);
+        wedge_acc(r, x, y);
+      }
+#pragma unroll
+      for (int e = 0; e < 9; ++e) r[e] = group_sum<TPS>(r[e]);
+      // out[n][m] = W[m][n] R for n = perm(m); every other block is zero.
+      for (int blk = sub; blk < 16; blk += TPS) {
+        const int n = blk / 4, m = blk % 4;
+        const bool hit = pw.perm[m] == n;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) st(out + blk * 9 + e, hit ? mul_phase(r[e], pw.ph[m]) : czero<R>());
+      }
+    } else {
+      field_blocks(b, pw, A, B, scratch, sub, out);
+    }
+  }
+
+  __device__ static void field_blocks(const BaryonSpin<R> &b, const ProjOperand<R> &pw, const S *A, const S *B,
+                                      const S *scratch, int sub, S *out)
+  {
+    for (int blk = sub; blk < 16; blk += TPS) {
+      cx<R> d[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) d[e] = czero<R>();
+      int dst;
+      if constexpr (LOOP) {
+        cx<R> q[9];
+        load9(q, scratch);
+        if constexpr (ROLE == 0) {  // block (i, k), k = perm2 l
+          const int i = blk / 4, k = blk % 4, l = b.perm2[k], j = b.perm1[i];
+          cx<R> y[9];
+          load9(y, B + (j * 4 + l) * 9);
+          phase9(y, (b.ph1[0][i] + b.ph2[0][l]) & 3u);
+          wedge_acc(d, y, q);
+        } else {  // block (j, l), i = perm1 j
+          const int j = blk / 4, l = blk % 4, i = b.perm1[j];
+          cx<R> x[9];
+          load9(x, A + (i * 4 + b.perm2[l]) * 9);
+          phase9(x, (b.ph1[0][i] + b.ph2[0][l]) & 3u);
+          wedge_acc(d, x, q);
+        }
+        dst = blk;
+      } else if constexpr (ROLE == 0) {  // block (i, k)
+        const int i = blk / 4, k = blk % 4, l = b.perm2[k], j = b.perm1[i];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          cx<R> y[9], nn[9];
+          load9(y, B + (j * 4 + m) * 9);
+          load9(nn, scratch + (m * 4 + l) * 9);
+          wedge_acc(d, y, nn);
+        }
+        phase9(d, (b.ph1[0][i] + b.ph2[0][l]) & 3u);
+        dst = blk;
+      } else if constexpr (ROLE == 1) {  // block (j, m), i = perm1 j
+        const int j = blk / 4, m = blk % 4, i = b.perm1[j];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+          cx<R> x[9], nn[9];
+          load9(x, A + (i * 4 + b.perm2[l]) * 9);
+          phase9(x, b.ph2[0][l]);
+          load9(nn, scratch + (m * 4 + l) * 9);
+          wedge_acc(d, x, nn);
+        }
+        phase9(d, b.ph1[0][i]);
+        dst = blk;
+      } else {  // ROLE 2, triangle: block (n, l), n = perm(m)
+        const int n = blk / 4, l = blk % 4, m = pw.perm[n];  // perm is an involution
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          cx<R> x[9], y[9];
+          load9(x, A + (i * 4 + b.perm2[l]) * 9);
+          load9(y, B + (b.perm1[i] * 4 + m) * 9);
+          phase9(x, b.ph1[0][i]);
+          wedge_acc(d, x, y);
+        }
+        phase9(d, (b.ph2[0][l] + pw.ph[m]) & 3u);
+        dst = blk;
+      }
+#pragma unroll
+      for (int e = 0; e < 9; ++e) st(out + dst * 9 + e, d[e]);
+    }
+  }
+};
+
+} // namespace cgb

@@ -1,0 +1,122 @@
+/*
+ * contract_gb300.h -- extensions of the libcontract.so C ABI (GB300 build).
+ *
+ * None of these entry points exists in CLQCD/contract; they add what its
+ * callers otherwise do themselves (per-timeslice sums, many contraction types
+ * per pass, precision choice) plus error reporting and stream control.
+ *
+ * Shared conventions (see also contract.h):
+ *  - precision: CONTRACT_C128 propagators are complex128 (the drop-in format);
+ *    CONTRACT_C64 propagators are complex64 and the arithmetic is FP32 with
+ *    FP64 per-timeslice reduction ("mixed" form).
+ *  - lattice: int[4] = {Lx, Ly, Lz, Lt} of the local lattice in PyQUDA
+ *    even/odd site order, site = (((p*Lt + t)*Lz + z)*Ly + y)*(Lx/2) + xh,
+ *    Lx even.  When a call takes `lattice`, passing NULL selects per-site
+ *    output (one complex128 per site, `volume` sites); non-NULL selects
+ *    per-timeslice sums (Lt complex128 values, the reduction in FP64).
+ *  - correlator outputs are always complex128 device buffers.
+ */
+#ifndef CONTRACT_GB300_H
+#define CONTRACT_GB300_H
+
+#include <stddef.h>
+
+#include "contract.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  CONTRACT_C128 = 0,
+  CONTRACT_C64 = 1,
+};
+
+/* ----------------------------------------------------------- errors ---- */
+enum {
+  CONTRACT_SUCCESS = 0,
+  CONTRACT_ERROR_INVALID_ARGUMENT = 1,
+  CONTRACT_ERROR_CUDA = 2,             /* a CUDA runtime call failed */
+  CONTRACT_ERROR_DEVICE_TIMEOUT = 3,   /* a kernel gave up waiting on its own copies */
+  CONTRACT_ERROR_OUT_OF_MEMORY = 4,    /* the workspace could not grow */
+  CONTRACT_ERROR_BAD_WORK = 5,         /* a batched work descriptor failed validation */
+};
+
+enum {
+  CONTRACT_ERRORS_EXIT = 0,    /* reference behaviour: message on stderr, exit(-1) (CUDA errors: exit(code)) */
+  CONTRACT_ERRORS_RECORD = 1,  /* record the error, skip the call, return */
+};
+
+/* Select how invalid calls are handled.  The default is CONTRACT_ERRORS_EXIT
+ * unless the environment variable CONTRACT_ERROR_MODE=record is set. */
+void contract_set_error_mode(int mode);
+int contract_get_error_mode(void);
+
+/* First error recorded since the last clear (sticky), and its message. */
+int contract_last_error(void);
+const char *contract_last_error_message(void);
+void contract_clear_error(void);
+
+/* Synchronise the current stream, then fold the device status word (errors
+ * reported by kernels, e.g. a timed-out wait) into the sticky error. */
+int contract_check_device(void);
+
+/* ---------------------------------------------------------- streams ---- */
+/* All later calls (drop-in ones included) queue work on `stream`
+ * (a cudaStream_t; NULL = legacy default stream, the reference's choice). */
+void contract_set_stream(void *stream);
+void *contract_get_stream(void);
+
+/* Reserve `bytes` of the per-device workspace used by per-timeslice
+ * reductions, so that later calls (e.g. inside CUDA graph capture) do not
+ * allocate.  Returns CONTRACT_SUCCESS or an error code. */
+int contract_workspace_reserve(size_t bytes);
+/* Workspace bytes a per-timeslice call with `noutputs` correlators needs. */
+size_t contract_workspace_bytes(const int *lattice, int noutputs);
+
+/* ------------------------------------------------------ gamma algebra -- */
+/* perm[16*4], phase[16*4]: Gamma(n)[r][perm[n*4+r]] = i^phase[n*4+r]. */
+void contract_gamma_table(int *perm, int *phase);
+
+/* ------------------------------------------------------- conversion ---- */
+/* complex128 <-> complex64 propagator copy of `volume` sites on the device. */
+void contract_convert_precision(void *dst, const void *src, size_t volume, int to_c64);
+
+/* ------------------------------------------------------ contractions --- */
+/* meson_two_point with a precision and optional per-timeslice output. */
+void contract_meson(void *correl, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
+                    int gamma_kl, int precision, const int *lattice);
+
+/* meson_all_{source,sink}_two_point: correl is a HOST array of 16 device
+ * pointers; `source` != 0 fixes gamma_ij = fixed_gamma and loops gamma_kl,
+ * else fixes gamma_kl and loops gamma_ij. */
+void contract_meson_all(void **correl, const void *propag_i, const void *propag_j, size_t volume, int fixed_gamma,
+                        int source, int precision, const int *lattice);
+
+/* baryon_two_point / baryon_general_two_point in one call: project_mn (HOST,
+ * 16 complex128, row-major) replaces Gamma(gamma_mn) when non-NULL. */
+void contract_baryon(void *correl, const void *propag_i, const void *propag_j, const void *propag_n,
+                     BaryonContractType contract_type, size_t volume, int gamma_ij, int gamma_kl, int gamma_mn,
+                     const void *project_mn, int precision, const int *lattice);
+
+/* All six contraction types for `nproj` (1 or 2) projectors in one pass over
+ * the three propagators.  projectors: HOST, nproj x 16 complex128.
+ * correl: device complex128 [6][nproj][Lt] (lattice given) or
+ * [6][nproj][volume] (lattice NULL); types in BaryonContractType order. */
+void contract_baryon_all_types(void *correl, const void *propag_i, const void *propag_j, const void *propag_n,
+                               size_t volume, int gamma_ij, int gamma_kl, int nproj, const void *projectors,
+                               int precision, const int *lattice);
+
+/* baryon_diquark / baryon_sequential_two_point with a storage precision
+ * (fields are read and written in that precision). */
+void contract_diquark(void *diquark, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
+                      int gamma_kl, int precision);
+void contract_sequential(void *propag_i, void *propag_j, void *propag_n, BaryonContractType contract_type,
+                         BaryonSequentialType sequential_type, size_t volume, int gamma_ij, int gamma_kl,
+                         int gamma_mn, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CONTRACT_GB300_H */

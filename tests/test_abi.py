@@ -1,0 +1,168 @@
+"""The C-ABI library without a GPU: it loads, exports every declared symbol,
+carries the reference's enum values and gamma tables, and rejects invalid
+calls the way the reference does."""
+import ctypes
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+INCLUDE = os.path.join(ROOT, "include")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from contract_gb300 import build
+    build.build()
+    from contract_gb300 import _lib
+    return _lib.lib()
+
+
+def declared_functions():
+    names = set()
+    for h in ("contract.h", "contract_gb300.h"):
+        src = open(os.path.join(INCLUDE, h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:void|int|size_t|const char|void \*)\s*\*?\s*(\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert {"init", "meson_two_point", "meson_all_source_two_point", "meson_all_sink_two_point", "baryon_diquark",
+            "baryon_two_point", "baryon_general_two_point", "baryon_sequential_two_point"} <= names
+    for n in names:
+        assert hasattr(lib, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", lib._name], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert names <= exported
+    # nothing but the C ABI leaks out of the library
+    assert exported == names, sorted(exported - names)
+
+
+def test_python_signatures_cover_the_headers():
+    from contract_gb300 import _lib
+    assert declared_functions() == set(_lib.SIGNATURES)
+
+
+def test_enum_values_match_contract_enum():
+    from contract_gb300.pycontract import BaryonContractType as T, BaryonSequentialType as S
+    src = open(os.path.join(INCLUDE, "contract_enum.h")).read()
+    body = src[src.index("typedef enum {"):src.index("} BaryonContractType;")]
+    values = {}
+    nxt = 0
+    for name, val in re.findall(r"(\w+)\s*(?:=\s*(\w+))?\s*,", body):
+        values[name] = values[val] if val else nxt
+        nxt = values[name] + 1
+    assert values["IM_JL_NK"] == 5 and values["IN_JK_ML"] == 4 and values["AF_BE_CD"] == 5
+    for name, v in values.items():
+        assert T[name] == v, name
+    assert (S.SEQUENTIAL_I, S.SEQUENTIAL_J, S.SEQUENTIAL_N) == (0, 1, 2)
+
+
+def test_enum_header_include_twice(tmp_path):
+    src = tmp_path / "t.c"
+    src.write_text('#include "contract_enum.h"\n#include "contract_enum.h"\n#include "contract_gb300.h"\n'
+                   "int main(void) { return IN_JL_MK == 5 ? 0 : 1; }\n")
+    r = subprocess.run(["gcc", "-std=c11", "-I", INCLUDE, str(src), "-o", str(tmp_path / "t")], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(tmp_path / "t")]).returncode == 0
+
+
+def test_gamma_table_bit_exact(lib, golden):
+    perm = (ctypes.c_int * 64)()
+    phase = (ctypes.c_int * 64)()
+    lib.contract_gamma_table(perm, phase)
+    perm = np.array(perm[:]).reshape(16, 4)
+    val = 1j ** np.array(phase[:]).reshape(16, 4)
+    assert np.array_equal(perm, golden["gamma_index"])
+    assert np.array_equal(np.round(val, 15), golden["gamma_data"])
+
+
+def test_decompose_gamma():
+    from contract_gb300 import pycontract as pc
+    g = pc.gamma_matrices()
+    c_g5 = g[2] @ g[8] @ g[15]  # C g5 = g2 g4 g5
+    n, c = pc.decompose_gamma(c_g5)
+    assert n == 5 and c == 1
+    n, c = pc.decompose_gamma(-1j * g[13])
+    assert n == 13 and abs(c + 1j) < 1e-15
+    with pytest.raises(ValueError):
+        pc.decompose_gamma((np.eye(4) + g[8]) / 2)
+
+
+def _run(code):
+    return subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT,
+                          env=dict(os.environ, PYTHONPATH=ROOT))
+
+
+def test_invalid_selector_exits_like_reference():
+    # baryon.cu:61-63 of the reference: "Error: Invalid contract_type value %d" then exit(-1).
+    r = _run("from contract_gb300 import _lib; L=_lib.lib(); "
+             "L.baryon_two_point(None,None,None,None,7,0,5,5,8); print('survived')")
+    assert r.returncode == 255 and "survived" not in r.stdout
+    assert "Invalid contract_type value 7" in r.stderr
+    r = _run("from contract_gb300 import _lib; L=_lib.lib(); "
+             "L.baryon_two_point(None,None,None,None,1,0,5,5,16); print('survived')")
+    assert r.returncode == 255 and "Invalid gamma_mn value 16" in r.stderr
+
+
+def test_silent_noops_like_reference():
+    # diquark.cu:40 and contract.cpp:60 of the reference ignore these selectors.
+    r = _run("from contract_gb300 import _lib; L=_lib.lib(); "
+             "L.baryon_diquark(None,None,None,0,17,5); "
+             "L.baryon_sequential_two_point(None,None,None,0,3,0,5,5,8); print('survived')")
+    assert r.returncode == 0 and "survived" in r.stdout
+
+
+def test_record_mode_reports_errors(lib):
+    lib.contract_set_error_mode(1)
+    try:
+        lib.contract_clear_error()
+        lib.baryon_two_point(None, None, None, None, 9, 0, 5, 5, 8)
+        assert lib.contract_last_error() == 1
+        assert b"Invalid contract_type value 9" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        lib.meson_two_point(None, None, None, 16, 5, 5)
+        assert lib.contract_last_error() == 1 and b"NULL" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        lat = (ctypes.c_int * 4)(3, 2, 2, 4)  # odd Lx
+        lib.contract_meson(None, None, None, 0, 5, 5, 0, lat)
+        assert lib.contract_last_error() == 1 and b"Lx even" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        lib.contract_baryon_all_types(None, None, None, None, 0, 5, 5, 3, None, 0, None)
+        assert lib.contract_last_error() == 1
+        lib.contract_clear_error()
+    finally:
+        lib.contract_set_error_mode(0)
+
+
+def test_pycontract_raises_on_invalid(lib):
+    from contract_gb300 import pycontract as pc
+    with pytest.raises(pc.ContractError, match="Invalid gamma_kl"):
+        pc.meson_two_point(0, 0, 0, 0, 3, 99)
+    lib.contract_set_error_mode(0)
+
+
+def test_workspace_bytes(lib):
+    lat = (ctypes.c_int * 4)(24, 24, 24, 64)
+    b = lib.contract_workspace_bytes(lat, 12)
+    assert b >= 884736 // 16 * 12 * 16  # one partial per (at least) 16-site tile
+
+
+def test_misaligned_pointer_rejected(lib):
+    lib.contract_set_error_mode(1)
+    try:
+        lib.contract_clear_error()
+        lib.meson_two_point(0x1008, 0x2000, 0x3000, 4, 5, 5)
+        assert lib.contract_last_error() == 1 and b"16-byte aligned" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+    finally:
+        lib.contract_set_error_mode(0)

@@ -1,0 +1,151 @@
+"""GPU kernels against the C oracle on seeded lattices larger than the golden
+fixtures: ragged tails, odd volumes, both precisions, per-site and
+per-timeslice outputs, and the fused all-types kernel."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import einsum_oracle as eo
+
+pytestmark = pytest.mark.gpu
+TOL_C128 = 1e-12           # plain form (FP64 throughout)
+TOL_C64_TIMESLICE = 1e-6   # mixed form: max relative error per timeslice vs the FP64 oracle
+
+LATT = (4, 4, 4, 8)
+
+
+@pytest.fixture(scope="module")
+def props():
+    pi = eo.make_propagator(LATT, 21, 0.25)
+    pj = eo.make_propagator(LATT, 22, 0.25)
+    pn = eo.make_propagator(LATT, 23, 0.30)
+    return pi, pj, pn
+
+
+@pytest.fixture(scope="module")
+def api():
+    from contract_gb300 import build
+    build.build()
+    from contract_gb300 import api, pycontract
+    pycontract.init(0)
+    return api
+
+
+def cuda(a, c64=False):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return t.to(torch.complex64) if c64 else t
+
+
+def per_t_rel(got, ref):
+    got, ref = np.asarray(got), np.asarray(ref)
+    return float(np.max(np.abs(got - ref) / np.abs(ref)))
+
+
+def test_ragged_volumes(api, props, c_oracle):
+    """Volumes that are not multiples of any tile (the reference needs volume % 4 == 0)."""
+    from contract_gb300 import pycontract as pc
+    for v in (1, 3, 37, 129, 200):
+        pi, pj, pn = [p[:v] for p in props]
+        got = pc.baryonTwoPoint(cuda(pi), cuda(pj), cuda(pn), 1, 5, 5, 8).cpu().numpy()
+        assert rel_err(got, c_oracle.baryon_two_point(pi, pj, pn, 1, 5, 5, 8)) < TOL_C128, v
+        got = pc.mesonTwoPoint(cuda(pi), cuda(pj), 15, 15).cpu().numpy()
+        assert rel_err(got, c_oracle.meson_two_point(pi, pj, 15, 15)) < TOL_C128, v
+
+
+def test_empty_volume(api):
+    import torch
+    from contract_gb300 import pycontract as pc
+    z = torch.empty((0, 4, 4, 3, 3), dtype=torch.complex128, device="cuda")
+    assert pc.mesonTwoPoint(z, z, 5, 5).numel() == 0
+    assert pc.baryonTwoPoint(z, z, z, 0, 5, 5, 8).numel() == 0
+
+
+def test_baryon_all_types_all_gammas_c128(api, props, c_oracle):
+    from contract_gb300 import pycontract as pc
+    pi, pj, pn = props
+    a, b, c = cuda(pi), cuda(pj), cuda(pn)
+    for gij, gkl in ((5, 5), (13, 13), (0, 15), (3, 10)):
+        for t in range(6):
+            for gmn in (0, 8, 4, 15):
+                got = pc.baryonTwoPoint(a, b, c, t, gij, gkl, gmn).cpu().numpy()
+                assert rel_err(got, c_oracle.baryon_two_point(pi, pj, pn, t, gij, gkl, gmn)) < TOL_C128
+
+
+def test_meson_all_per_timeslice(api, props, c_oracle):
+    pi, pj, _ = props
+    got = api.meson_all_timeslice(cuda(pi), cuda(pj), LATT, 5, source=True).cpu().numpy()
+    ref = eo.timeslice_sum(c_oracle.meson_all_source(pi, pj, 5), LATT)
+    assert rel_err(got, ref) < TOL_C128
+    got64 = api.meson_all_timeslice(cuda(pi, True), cuda(pj, True), LATT, 5, source=True).cpu().numpy()
+    for g in range(16):
+        assert per_t_rel(got64[g], ref[g]) < TOL_C64_TIMESLICE, g
+
+
+def test_baryon_timeslice_both_precisions(api, props, c_oracle):
+    pi, pj, pn = props
+    pp = api.projector_plus_minus()
+    for t in range(6):
+        ref = eo.timeslice_sum(c_oracle.baryon_general_two_point(pi, pj, pn, t, 5, 5, pp[0]), LATT)
+        got = api.baryon(cuda(pi), cuda(pj), cuda(pn), t, 5, 5, project_mn=pp[0], latt=LATT).cpu().numpy()
+        assert rel_err(got, ref) < TOL_C128, t
+        got64 = api.baryon(cuda(pi, True), cuda(pj, True), cuda(pn, True), t, 5, 5, project_mn=pp[0],
+                           latt=LATT).cpu().numpy()
+        assert per_t_rel(got64, ref) < TOL_C64_TIMESLICE, t
+
+
+def test_fused_all_types(api, props, c_oracle):
+    pi, pj, pn = props
+    pp = api.projector_plus_minus()
+    ref = np.zeros((6, 2, LATT[3]), np.complex128)
+    ref_site = np.zeros((6, 2, pi.shape[0]), np.complex128)
+    for t in range(6):
+        for w in range(2):
+            ref_site[t, w] = c_oracle.baryon_general_two_point(pi, pj, pn, t, 5, 5, pp[w])
+            ref[t, w] = eo.timeslice_sum(ref_site[t, w], LATT)
+    got = api.baryon_all_types(cuda(pi), cuda(pj), cuda(pn), 5, 5, pp, latt=LATT).cpu().numpy()
+    assert rel_err(got, ref) < TOL_C128
+    got_site = api.baryon_all_types(cuda(pi), cuda(pj), cuda(pn), 5, 5, pp).cpu().numpy()
+    assert rel_err(got_site, ref_site) < TOL_C128
+    got1 = api.baryon_all_types(cuda(pi), cuda(pj), cuda(pn), 5, 5, pp[:1], latt=LATT).cpu().numpy()
+    assert rel_err(got1[:, 0], ref[:, 0]) < TOL_C128
+    got64 = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp, latt=LATT).cpu().numpy()
+    for t in range(6):
+        for w in range(2):
+            assert per_t_rel(got64[t, w], ref[t, w]) < TOL_C64_TIMESLICE, (t, w)
+
+
+def test_mixed_field_ops(api, props, c_oracle):
+    """complex64 diquark/sequential fields: elementwise error at FP32 level."""
+    import torch
+    from contract_gb300 import pycontract as pc
+    pi, pj, pn = [p[:64] for p in props]
+    ref = c_oracle.baryon_diquark(pi, pj, 5, 5)
+    got = pc.baryonDiquark(cuda(pi, True), cuda(pj, True), 5, 5).to(torch.complex128).cpu().numpy()
+    assert rel_err(got, ref) < 1e-6
+    for t in range(6):
+        for s in range(3):
+            ref = c_oracle.baryon_sequential(pi, pj, pn, t, s, 5, 5, 8)
+            bufs = [cuda(p, True) for p in (pi, pj, pn)]
+            pc.baryonSequentialTwoPoint(*bufs, t, s, 5, 5, 8)
+            assert rel_err(bufs[s].to(torch.complex128).cpu().numpy(), ref) < 1e-6, (t, s)
+
+
+def test_precision_conversion_roundtrip(api, props):
+    import torch
+    pi = cuda(props[0])
+    lo = api.to_c64(pi)
+    assert torch.equal(lo, pi.to(torch.complex64))
+    assert torch.equal(api.to_c128(lo), lo.to(torch.complex128))
+
+
+def test_timeslice_deterministic(api, props):
+    pi, pj, pn = props
+    pp = api.projector_plus_minus()
+    a = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp, latt=LATT)
+    b = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp, latt=LATT)
+    assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
+def test_device_status_clean(api):
+    api.check_device()
