@@ -1,0 +1,391 @@
+"""Benchmark: baryon two-point contractions on a 24^3 x 64 lattice (one GB300).
+
+Workload ("baryon_2pt_24c64"): three propagators u, u, d in PyQUDA even/odd
+layout [2, 64, 24, 24, 12, 4, 4, 3, 3] -- seeded unit-variance complex Gaussian
+entries times exp(-m|t|) (m = 0.25, 0.25, 0.30; the two u propagators hold the
+same values in separate buffers, d has its own seed).  One step evaluates all
+six contract_enum.h contraction types with Gamma_ij = Gamma_kl = C g5
+(Gamma(5)) for the two projectors (1 +- g4)/2 at zero momentum, i.e. 12
+site-contractions per site, reduced per timeslice.
+
+Metric: GSite/s = site-contractions per second / 1e9 for the mixed form
+(complex64 storage, FP32 arithmetic, FP64 per-timeslice reduction) with the
+propagators resident in HBM; the plain complex128 form, per-call and fused, is
+measured beside it, and the per-timeslice relative error of the mixed form
+against the plain FP64 form is reported.  ``e2e`` repeats the measurement
+through the C ABI from pinned host complex128 buffers, with the host->device
+copies, the complex128->complex64 conversion and the read-back of the
+correlators inside the timed region.
+
+``--impl reference`` times the reference's CPU arithmetic for the same
+workload on the host cores (see ``oracle/``).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LATT = (24, 24, 24, 64)
+MASSES = (0.25, 0.25, 0.30)
+GAMMA_CG5 = 5
+N_TYPES = 6
+N_PROJ = 2
+UNITS_PER_SITE = N_TYPES * N_PROJ
+# FP32 operations per site of the fused kernel (loop form 576 complex FMA
+# + 2 triangles x 2 projectors x 2448 complex FMA + projector/Q set-up), 8 flops per complex FMA.
+FUSED_CFMA_PER_SITE = 576 + 4 * 2448 + 2 * 9 * 8
+WORKLOAD = "baryon_2pt_24c64"
+METRIC = "GSite/s & HBM GB/s: mixed vs FP64 GPU contraction at <=1e-6 rel err/timeslice"
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the fused kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "baryon_fused_c64_24c64.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ CPU baseline --
+
+def cpu_reference(steps, warmup, sample_slices):
+    """Reference CPU arithmetic on a bounded sample (`sample_slices` timeslices)."""
+    from oracle import einsum_oracle as eo
+    from oracle import lib as L
+    L.build()
+    impl, kind = L.ref_oracle(), "reference"
+    if impl is None:
+        impl, kind = L.c_oracle(), "port"
+    lx, ly, lz, lt = LATT
+    sub = (lx, ly, lz, sample_slices)
+    pu = eo.make_propagator(sub, 1, MASSES[0])
+    pd = eo.make_propagator(sub, 3, MASSES[2])
+    g4 = eo.GAMMA[8]
+    projs = [((np.eye(4) + g4) / 2).reshape(16), ((np.eye(4) - g4) / 2).reshape(16)]
+    v = pu.shape[0]
+
+    def step():
+        for t in range(N_TYPES):
+            for p in projs:
+                impl.baryon_general_two_point(pu, pu, pd, t, GAMMA_CG5, GAMMA_CG5, p)
+
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    value = v * UNITS_PER_SITE / dt / 1e9
+    return {"value": value, "unit": "GSite/s", "cores": cores, "kind": kind,
+            "sample": f"{sample_slices} of {lt} timeslices ({v} sites) x 6 types x 2 projectors, FP64, OpenMP",
+            "seconds_per_step": dt}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    cb = cpu_reference(args.steps, args.warmup, args.cpu_slices)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GSite/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["seconds_per_step"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "lattice": list(LATT), "sample": cb["sample"]},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": "GSite/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU arm --
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from contract_gb300 import api, build
+    from contract_gb300 import _lib
+    from contract_gb300.lattice import synthetic_propagator
+
+    torch.cuda.set_device(local)
+    build.build()
+    lib = _lib.lib()
+    lib.contract_set_error_mode(1)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    lib.contract_set_stream(stream.cuda_stream)
+
+    lx, ly, lz, lt = LATT
+    v = lx * ly * lz * lt
+    units = v * UNITS_PER_SITE
+    latt_c = (ctypes.c_int * 4)(*LATT)
+    projs = np.ascontiguousarray(api.projector_plus_minus())
+    proj_ptr = projs.ctypes.data
+
+    # resident inputs (complex128 drop-in format) and the mixed-form copies
+    u = synthetic_propagator(LATT, 1000 + rank, MASSES[0], device=dev)
+    u2 = u.clone()
+    d = synthetic_propagator(LATT, 3000 + rank, MASSES[2], device=dev)
+    u64, u264, d64 = api.to_c64(u), api.to_c64(u2), api.to_c64(d)
+    out64 = torch.empty((N_TYPES, N_PROJ, lt), dtype=torch.complex128, device=dev)
+    out128 = torch.empty_like(out64)
+    lib.contract_workspace_reserve(lib.contract_workspace_bytes(latt_c, UNITS_PER_SITE))
+
+    def fused(out, a, b, c, prec):
+        lib.contract_baryon_all_types(out.data_ptr(), a.data_ptr(), b.data_ptr(), c.data_ptr(), v, GAMMA_CG5,
+                                      GAMMA_CG5, N_PROJ, proj_ptr, prec, latt_c)
+
+    def check():
+        if lib.contract_last_error():
+            raise RuntimeError(lib.contract_last_error_message().decode())
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        check()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        check()
+        return e0.elapsed_time(e1) / steps  # ms
+
+    # ---- headline: mixed fused, inputs resident (3 x 1.02 GB > L2, no flush needed)
+    with ClockSampler(local) as clocks:
+        ms_mixed = timed(lambda: fused(out64, u64, u264, d64, 1), args.steps, args.warmup)
+    ms_mixed = max_over_ranks(ms_mixed, world, dev)
+    value = world * units / (ms_mixed * 1e-3) / 1e9
+
+    # ---- plain complex128 forms: fused, and the drop-in per-call sequence
+    plain_steps = max(1, min(args.steps, 5))
+    ms_plain_fused = timed(lambda: fused(out128, u, u2, d, 0), plain_steps, 1)
+    corr_t = torch.empty(lt, dtype=torch.complex128, device=dev)
+
+    def per_call():
+        for t in range(N_TYPES):
+            for w in range(N_PROJ):
+                lib.contract_baryon(corr_t.data_ptr(), u.data_ptr(), u2.data_ptr(), d.data_ptr(), t, v, GAMMA_CG5,
+                                    GAMMA_CG5, 0, projs[w].ctypes.data, 0, latt_c)
+
+    ms_plain_call = timed(per_call, max(1, min(args.steps, 2)), 1)
+    per_call_mixed = lambda: [lib.contract_baryon(corr_t.data_ptr(), u64.data_ptr(), u264.data_ptr(),  # noqa: E731
+                                                  d64.data_ptr(), t, v, GAMMA_CG5, GAMMA_CG5, 0,
+                                                  projs[w].ctypes.data, 1, latt_c)
+                              for t in range(N_TYPES) for w in range(N_PROJ)]
+    ms_mixed_call = timed(per_call_mixed, max(1, min(args.steps, 5)), 1)
+
+    # ---- accuracy of the mixed form per timeslice (vs the FP64 GPU form,
+    # which the tests pin to the FP64 oracle)
+    fused(out64, u64, u264, d64, 1)
+    fused(out128, u, u2, d, 0)
+    # FP64 contraction of the complex64-rounded inputs: the share of the error
+    # that storage rounding alone causes
+    out_rnd = torch.empty_like(out128)
+    fused(out_rnd, *[api.to_c128(x) for x in (u64, u264, d64)], 0)
+    torch.cuda.synchronize(dev)
+    a, b, r = out64.cpu().numpy(), out128.cpu().numpy(), out_rnd.cpu().numpy()
+    rel = np.abs(a - b) / np.abs(b)
+    rel_in = np.abs(r - b) / np.abs(b)
+    acc = {"max_rel_err_per_timeslice": float(rel.max()),
+           "median_rel_err_per_timeslice": float(np.median(rel)),
+           "max_rel_err_by_type": [float(rel[t].max()) for t in range(N_TYPES)],
+           "frac_timeslices_le_1e-6": float((rel <= 1e-6).mean()),
+           "input_rounding_only": {"max_rel_err_per_timeslice": float(rel_in.max()),
+                                   "median_rel_err_per_timeslice": float(np.median(rel_in))}}
+
+    # ---- e2e through the C ABI from pinned host complex128 buffers
+    host = [x.cpu().pin_memory() for x in (u, u2, d)]
+    dev_in = [torch.empty_like(u) for _ in range(3)]
+    dev64 = [torch.empty(u.shape, dtype=torch.complex64, device=dev) for _ in range(3)]
+    host_out = torch.empty(out64.shape, dtype=out64.dtype).pin_memory()
+
+    def e2e_step():
+        for h, dv, d64_ in zip(host, dev_in, dev64):
+            dv.copy_(h, non_blocking=True)
+            lib.contract_convert_precision(d64_.data_ptr(), dv.data_ptr(), v, 1)
+        fused(out64, *dev64, 1)
+        host_out.copy_(out64, non_blocking=True)
+
+    e2e_steps = max(1, min(args.steps, 5))
+    ms_e2e = timed(e2e_step, e2e_steps, 1)
+    ms_e2e = max_over_ranks(ms_e2e, world, dev)
+    h2d = sum(x.numel() * x.element_size() for x in host)
+    d2h = host_out.numel() * host_out.element_size()
+
+    # ---- roofline of the dominant kernel (fused mixed): algorithmic bytes / time
+    hbm_peak, peak_kind = peaks()
+    bytes_per_launch = 3 * v * 1152 + N_TYPES * N_PROJ * lt * 16
+    achieved = bytes_per_launch / (ms_mixed * 1e-3) / 1e9
+    flops_per_launch = 8.0 * FUSED_CFMA_PER_SITE * v
+    traffic = ncu_traffic()
+
+    result = None
+    if rank == 0:
+        cb = cpu_reference(1, 0, args.cpu_slices) if not args.no_cpu else None
+        result = {
+            "metric": METRIC, "value": value, "unit": "GSite/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64/f32 (f64 timeslice reduction)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "lattice": list(LATT), "propagators": "u,u,d c64 resident",
+                       "masses": list(MASSES), "gamma_ij": "C g5 = Gamma(5)", "gamma_kl": "C g5 = Gamma(5)",
+                       "projectors": "(1+g4)/2, (1-g4)/2", "types": 6, "site_contractions_per_step": units,
+                       "l2": "inputs 3.06 GB > L2 129 MB, no flush", "parallelism": f"replicas x{world}"},
+            "hbm_gbs": achieved,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "scalar_kernel<BaryonFusedOp<float,float2,...,NW=2>> + finalize",
+                         "algorithmic_bytes_per_launch": bytes_per_launch},
+            "fp32_pipe": {"achieved_tflops": flops_per_launch / (ms_mixed * 1e-3) / 1e12,
+                          "peak_tflops": 73.1, "peak_source": "measured FFMA probe",
+                          "frac": flops_per_launch / (ms_mixed * 1e-3) / 1e12 / 73.1},
+            "plain_c128": {"fused_ms": ms_plain_fused, "fused_gsite_s": units / (ms_plain_fused * 1e-3) / 1e9,
+                           "per_call_ms": ms_plain_call, "per_call_gsite_s": units / (ms_plain_call * 1e-3) / 1e9},
+            "mixed_per_call": {"ms": ms_mixed_call, "gsite_s": units / (ms_mixed_call * 1e-3) / 1e9,
+                               "hbm_gbs": 12 * 3 * v * 1152 / (ms_mixed_call * 1e-3) / 1e9},
+            "speedup_mixed_vs_plain_per_call": ms_plain_call / ms_mixed,
+            "accuracy": acc,
+            "e2e": {"value": world * units / (ms_e2e * 1e-3) / 1e9, "unit": "GSite/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clocks.summary(),
+            "cpu_baseline": None if cb is None else {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        }
+        print(json.dumps(result), flush=True)
+    return result
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--cpu-slices", type=int, default=8, help="timeslices in the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    world, rank, local = dist_setup(args)
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank)
+        else:
+            run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -507,10 +507,10 @@ size_t contract_workspace_bytes(const int *lattice, int noutputs)
 {
   if (!lattice || noutputs <= 0) return 0;
   const long long half = (long long)lattice[0] * lattice[1] * lattice[2] / 2;
-  // Upper bound over the tile shapes in use (smallest tile: 8 sites, one
-  // partial per chunk of at least one tile).
-  const long long tiles = (half + 7) / 8 * 2 * lattice[3];
-  return (size_t)tiles * noutputs * 16;
+  // One partial per (chunk, consumer warp): a chunk holds at least one tile of
+  // CW * SPW sites with SPW >= 2 and CW <= 16, so a half-timeslice yields at
+  // most half/2 + 16 partials.
+  return (size_t)(half / 2 + 16) * 2 * lattice[3] * noutputs * 16;
 }
 
 int contract_workspace_reserve(size_t bytes)

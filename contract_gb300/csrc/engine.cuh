@@ -12,23 +12,29 @@
 //
 // Data movement
 // -------------
-// Each site of each input propagator (144 complex: 2304 B in complex128,
-// 1152 B in complex64) is one cp.async.bulk (TMA) copy into its own padded
-// shared-memory slot (+16 B, which staggers consecutive sites across banks).
-// Thread 0 arms an mbarrier per stage with the expected byte count; all
-// threads wait on it with a time limit.  A timed-out wait sets a bit in the
-// device status word, drains this CTA's outstanding copies (again with a time
-// limit) and returns: no trap, no unbounded spin.
+// Warp 0 of every CTA is the producer: for each tile it waits until the ring
+// stage is free (`empty` mbarrier, one arrival per consumer warp), arms the
+// stage's `full` mbarrier with the tile's byte count and has its 32 lanes
+// issue the tile's cp.async.bulk (TMA) copies -- one per site and input, each
+// into its own padded shared-memory slot (+16 B, which staggers consecutive
+// sites across banks).  The CW consumer warps each own SPW = 32/TPS sites of
+// every tile; they wait on `full`, compute, and release the stage.  Warps
+// never meet at a CTA-wide barrier, so a slow warp only delays itself.
+//
+// Every wait is bounded in wall time.  A timed-out wait sets a bit in the
+// device status word and a CTA-local abort flag, waits (bounded again) for
+// the copies that may still be in flight into this CTA's shared memory, and
+// returns: no trap, no unbounded spin.
 //
 // Outputs
 // -------
 // Scalar ops (mesons, baryons) produce NOUT complex numbers per site: either
-// written per site (the reference's per-site output) or summed in FP64 per
-// chunk into `partial[chunk][NOUT]`, which `finalize_segments` reduces per
-// timeslice in a fixed order (deterministic).
+// written per site (the reference's per-site output) or summed per warp and
+// accumulated in FP64 per chunk into `partial[chunk][warp][NOUT]`, which
+// `finalize_kernel` reduces per timeslice in a fixed order (deterministic).
 // Field ops (diquark, sequential sources) produce a propagator-shaped site:
-// threads write it to a shared-memory staging slot, and thread 0 stores the
-// tile with cp.async.bulk shared->global copies (double-buffered).
+// lanes write it to a per-warp shared-memory staging slot (double-buffered)
+// and lane 0 stores it with cp.async.bulk shared->global copies.
 #pragma once
 
 #include "common.cuh"
@@ -82,215 +88,246 @@ template <class S> struct SiteLayout {
   static constexpr uint32_t SLOT = SITE_BYTES + 16;
 };
 
-// Shared-memory bytes used by the engines (op scratch excluded).
-template <class Op> constexpr size_t engine_smem_bytes()
-{
+// Shared-memory map of an engine kernel:
+//   [0, 128)        full[NST], empty[NST] mbarriers, abort flag
+//   stages          NST x NIN x SITES slots
+//   extra           SITES x EXTRA_SLOTS slots (per-site op scratch)
+//   tail            scalar ops: per-warp site values [CW][SPW][NOUT] (cx<R>)
+//                   field ops:  per-warp output staging [CW][2][SPW] slots
+template <class Op> struct Smem {
   using L = SiteLayout<typename Op::S>;
-  size_t b = 128 + (size_t)Op::NST * Op::NIN * Op::SITES * L::SLOT;
-  b += (size_t)Op::EXTRA_SLOTS * Op::SITES * L::SLOT;
-  if constexpr (Op::FIELD) b += 2ull * Op::SITES * L::SLOT;
-  else b += 2ull * Op::SITES * Op::NOUT * sizeof(double2);
-  return b;
+  static constexpr size_t STAGE = (size_t)Op::NIN * Op::SITES * L::SLOT;
+  static constexpr size_t STAGES = 128;
+  static constexpr size_t EXTRA = STAGES + Op::NST * STAGE;
+  static constexpr size_t TAIL = EXTRA + (size_t)Op::EXTRA_SLOTS * Op::SITES * L::SLOT;
+  static constexpr size_t tail_bytes()
+  {
+    if constexpr (Op::FIELD) return 2ull * Op::SITES * L::SLOT;
+    else return (size_t)Op::SITES * Op::NOUT * 2 * sizeof(typename Op::R);
+  }
+  static constexpr size_t BYTES = TAIL + tail_bytes();
+  static_assert(2 * Op::NST * 8 + 4 <= 128, "too many stages for the barrier block");
+};
+
+template <class Op> constexpr size_t engine_smem_bytes() { return Smem<Op>::BYTES; }
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// Issue the bulk copies of one tile into `stage` (called by one thread).
+// Producer warp: stream this CTA's tiles into the ring.
 template <class Op>
-__device__ __forceinline__ void issue_tile(const typename Op::Params &p, unsigned char *stage_ptr, uint64_t *bar,
-                                           long long first, int n)
+__device__ __forceinline__ void produce(const typename Op::Params &p, unsigned char *smem, uint64_t *full,
+                                        uint64_t *empty, volatile int *abort_flag)
 {
   using L = SiteLayout<typename Op::S>;
-  mbar_arrive_expect_tx(bar, (uint32_t)n * Op::NIN * L::SITE_BYTES);
-  for (int q = 0; q < Op::NIN; ++q) {
-    const char *src = static_cast<const char *>(p.in[q]) + first * L::SITE_BYTES;
-    unsigned char *dst = stage_ptr + (size_t)q * Op::SITES * L::SLOT;
-    for (int s = 0; s < n; ++s) bulk_g2s(dst + (size_t)s * L::SLOT, src + (size_t)s * L::SITE_BYTES, L::SITE_BYTES, bar);
+  constexpr int NST = Op::NST, NIN = Op::NIN, SITES = Op::SITES;
+  const TileGeom &g = p.geom;
+  const int lane = threadIdx.x & 31;
+  TileIter<SITES> it;
+  it.set_chunk(g, blockIdx.x);
+  for (int u = 0; it.valid(g); ++u) {
+    const int stage = u % NST;
+    if (u >= NST) {
+      const bool ok = mbar_wait_bounded(&empty[stage], ((u / NST) - 1) & 1, kWaitLimitNs);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) {
+          *abort_flag = 1;
+          report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
+        }
+        return;
+      }
+    }
+    if (*abort_flag) return;
+    long long first;
+    int n;
+    it.sites(g, first, n);
+    if (lane == 0) mbar_arrive_expect_tx(&full[stage], (uint32_t)n * NIN * L::SITE_BYTES);
+    __syncwarp();
+    unsigned char *dst = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
+    for (int c = lane; c < n * NIN; c += 32) {
+      const int q = c / n, s = c - q * n;
+      bulk_g2s(dst + ((size_t)q * SITES + s) * L::SLOT,
+               static_cast<const char *>(p.in[q]) + (first + s) * L::SITE_BYTES, L::SITE_BYTES, &full[stage]);
+    }
+    it.next(g);
   }
 }
 
-// Wait (bounded) for the copies of tiles [from, issued) so none is still
-// writing this CTA's shared memory when it exits after an error.
-template <int NST> __device__ void drain(uint64_t *full, int from, int issued)
+// A consumer warp that gave up: wait (bounded) for the copies of the next
+// NST-1 tiles, which the producer may already have issued.
+template <int NST> __device__ void drain(uint64_t *full, int from)
 {
-  for (int u = from; u < issued; ++u) mbar_wait_bounded(&full[u % NST], (u / NST) & 1, kWaitLimitNs / 4);
+  for (int u = from; u < from + NST; ++u) mbar_wait_bounded(&full[u % NST], (u / NST) & 1, kWaitLimitNs / 8);
 }
 
 // ------------------------------------------------------------ scalar ops --
-template <class Op> __global__ void __launch_bounds__(Op::THREADS, 1) scalar_kernel(const __grid_constant__ typename Op::Params p)
+template <class Op>
+__global__ void __launch_bounds__(Op::THREADS, 1) scalar_kernel(const __grid_constant__ typename Op::Params p)
 {
   using S = typename Op::S;
   using R = typename Op::R;
   using L = SiteLayout<S>;
   constexpr int NIN = Op::NIN, SITES = Op::SITES, TPS = Op::TPS, NST = Op::NST, NOUT = Op::NOUT;
-  constexpr size_t STAGE = (size_t)NIN * SITES * L::SLOT;
+  constexpr int SPW = 32 / TPS, CW = Op::CW;
 
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
-  unsigned char *stages = smem + 128;
-  unsigned char *extra = stages + NST * STAGE;
-  double2 *tile_vals = reinterpret_cast<double2 *>(extra + (size_t)Op::EXTRA_SLOTS * SITES * L::SLOT);
-
-  const TileGeom &g = p.geom;
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    for (int s = 0; s < NST; ++s) mbar_init(&full[s], 1);
+  uint64_t *empty = full + NST;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 120);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], CW);
+    }
+    *abort_flag = 0;
     fence_barrier_init();
   }
   __syncthreads();
-
-  TileIter<SITES> prod, cons;
-  prod.set_chunk(g, blockIdx.x);
-  cons.set_chunk(g, blockIdx.x);
-  int issued = 0;
-  if (tid == 0) {
-    for (int s = 0; s < NST && prod.valid(g); ++s) {
-      long long f;
-      int n;
-      prod.sites(g, f, n);
-      issue_tile<Op>(p, stages + s * STAGE, &full[s], f, n);
-      prod.next(g);
-      ++issued;
-    }
+  if (warp == 0) {
+    produce<Op>(p, smem, full, empty, abort_flag);
+    return;
   }
 
-  const int site = tid / TPS, sub = tid % TPS;
-  double2 chunk_acc = make_double2(0.0, 0.0);
-  for (int it = 0; cons.valid(g); ++it) {
-    const int stage = it % NST;
+  const TileGeom &g = p.geom;
+  const int w = warp - 1;
+  const int local = lane / TPS, sub = lane % TPS;
+  const int site = w * SPW + local;
+  cx<R> *sv = reinterpret_cast<cx<R> *>(smem + Smem<Op>::TAIL) + (size_t)w * SPW * NOUT;  // [SPW][NOUT]
+  S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_SLOTS * L::SLOT);
+  double2 chunk_acc = make_double2(0.0, 0.0);  // lane o < NOUT: output o
+
+  TileIter<SITES> it;
+  it.set_chunk(g, blockIdx.x);
+  for (int u = 0; it.valid(g); ++u) {
+    const int stage = u % NST;
     long long first;
     int n;
-    cons.sites(g, first, n);
-    const bool ok = mbar_wait_bounded(&full[stage], (it / NST) & 1, kWaitLimitNs);
-
-    const unsigned char *sb = stages + stage * STAGE;
+    it.sites(g, first, n);
+    const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, kWaitLimitNs);
+    if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
+      if (lane == 0) {
+        *abort_flag = 1;
+        report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
+        drain<NST>(full, u);
+      }
+      return;
+    }
+    const unsigned char *sb = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
     const S *in[NIN];
 #pragma unroll
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
     cx<R> vals[NOUT];
-    Op::site(p, in, reinterpret_cast<S *>(extra + (size_t)site * Op::EXTRA_SLOTS * L::SLOT), sub, vals);
+    Op::site(p, in, scratch, sub, vals);
 #pragma unroll
     for (int o = 0; o < NOUT; ++o) vals[o] = group_sum<TPS>(vals[o]);
-    if (sub == 0 && site < n) {
-      if (g.per_site) {
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[stage]);  // inputs consumed; only registers below
+    const bool valid = site < n;
+    if (g.per_site) {
+      if (sub == 0 && valid) {
 #pragma unroll
         for (int o = 0; o < NOUT; ++o)
           static_cast<double2 *>(p.out[o])[first + site] = make_double2(double(vals[o].x), double(vals[o].y));
-      } else {
+      }
+    } else {
+      if (sub == 0) {
 #pragma unroll
-        for (int o = 0; o < NOUT; ++o)
-          tile_vals[((it & 1) * SITES + site) * NOUT + o] = make_double2(double(vals[o].x), double(vals[o].y));
+        for (int o = 0; o < NOUT; ++o) sv[local * NOUT + o] = valid ? vals[o] : czero<R>();
       }
-    }
-    if (!__syncthreads_and(ok)) {
-      if (tid == 0) {
-        report(p.status, kDevErrWaitTimeout, (unsigned int)cons.chunk);
-        drain<NST>(full, it, issued);
+      __syncwarp();
+      if (lane < NOUT) {
+        cx<R> t = sv[lane];
+#pragma unroll
+        for (int s = 1; s < SPW; ++s) t = cadd(t, sv[s * NOUT + lane]);
+        chunk_acc.x += double(t.x);
+        chunk_acc.y += double(t.y);
+        if (it.last_in_chunk()) {
+          static_cast<double2 *>(p.out[0])[((size_t)it.chunk * CW + w) * NOUT + lane] = chunk_acc;
+          chunk_acc = make_double2(0.0, 0.0);
+        }
       }
-      return;
+      __syncwarp();
     }
-    if (!g.per_site && tid < NOUT) {
-      for (int s = 0; s < n; ++s) {
-        const double2 v = tile_vals[((it & 1) * SITES + s) * NOUT + tid];
-        chunk_acc.x += v.x;
-        chunk_acc.y += v.y;
-      }
-      if (cons.last_in_chunk()) {
-        static_cast<double2 *>(p.out[0])[(size_t)cons.chunk * NOUT + tid] = chunk_acc;
-        chunk_acc = make_double2(0.0, 0.0);
-      }
-    }
-    if (tid == 0 && prod.valid(g)) {
-      long long f;
-      int nn;
-      prod.sites(g, f, nn);
-      issue_tile<Op>(p, stages + stage * STAGE, &full[stage], f, nn);
-      prod.next(g);
-      ++issued;
-    }
-    cons.next(g);
+    it.next(g);
   }
 }
 
 // ------------------------------------------------------------- field ops --
-template <class Op> __global__ void __launch_bounds__(Op::THREADS, 1) field_kernel(const __grid_constant__ typename Op::Params p)
+template <class Op>
+__global__ void __launch_bounds__(Op::THREADS, 1) field_kernel(const __grid_constant__ typename Op::Params p)
 {
   using S = typename Op::S;
   using L = SiteLayout<S>;
   constexpr int NIN = Op::NIN, SITES = Op::SITES, TPS = Op::TPS, NST = Op::NST;
-  constexpr size_t STAGE = (size_t)NIN * SITES * L::SLOT;
+  constexpr int SPW = 32 / TPS, CW = Op::CW;
 
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
-  unsigned char *stages = smem + 128;
-  unsigned char *extra = stages + NST * STAGE;
-  unsigned char *outbuf = extra + (size_t)Op::EXTRA_SLOTS * SITES * L::SLOT;  // [2][SITES][SLOT]
-
-  const TileGeom &g = p.geom;
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    for (int s = 0; s < NST; ++s) mbar_init(&full[s], 1);
+  uint64_t *empty = full + NST;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 120);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], CW);
+    }
+    *abort_flag = 0;
     fence_barrier_init();
   }
   __syncthreads();
-
-  TileIter<SITES> prod, cons;
-  prod.set_chunk(g, blockIdx.x);
-  cons.set_chunk(g, blockIdx.x);
-  int issued = 0;
-  if (tid == 0) {
-    for (int s = 0; s < NST && prod.valid(g); ++s) {
-      long long f;
-      int n;
-      prod.sites(g, f, n);
-      issue_tile<Op>(p, stages + s * STAGE, &full[s], f, n);
-      prod.next(g);
-      ++issued;
-    }
+  if (warp == 0) {
+    produce<Op>(p, smem, full, empty, abort_flag);
+    return;
   }
 
-  const int site = tid / TPS, sub = tid % TPS;
-  for (int it = 0; cons.valid(g); ++it) {
-    const int stage = it % NST;
+  const TileGeom &g = p.geom;
+  const int w = warp - 1;
+  const int local = lane / TPS, sub = lane % TPS;
+  const int site = w * SPW + local;
+  S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_SLOTS * L::SLOT);
+  unsigned char *outbuf = smem + Smem<Op>::TAIL + (size_t)w * 2 * SPW * L::SLOT;  // [2][SPW] slots
+
+  TileIter<SITES> it;
+  it.set_chunk(g, blockIdx.x);
+  for (int u = 0; it.valid(g); ++u) {
+    const int stage = u % NST;
     long long first;
     int n;
-    cons.sites(g, first, n);
-    const bool ok = mbar_wait_bounded(&full[stage], (it / NST) & 1, kWaitLimitNs);
-
-    const unsigned char *sb = stages + stage * STAGE;
-    const S *in[NIN];
-#pragma unroll
-    for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
-    S *out = reinterpret_cast<S *>(outbuf + ((size_t)(it & 1) * SITES + site) * L::SLOT);
-    Op::site(p, in, reinterpret_cast<S *>(extra + (size_t)site * Op::EXTRA_SLOTS * L::SLOT), sub, out);
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      if (ok) {
-        for (int s = 0; s < n; ++s)
-          bulk_s2g(static_cast<char *>(p.out[0]) + (first + s) * L::SITE_BYTES,
-                   outbuf + ((size_t)(it & 1) * SITES + s) * L::SLOT, L::SITE_BYTES);
-      }
-      bulk_commit();
-      bulk_wait_read<1>();  // the other staging buffer is free again
-    }
-    if (!__syncthreads_and(ok)) {
-      if (tid == 0) {
-        report(p.status, kDevErrWaitTimeout, (unsigned int)cons.chunk);
-        drain<NST>(full, it, issued);
+    it.sites(g, first, n);
+    const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, kWaitLimitNs);
+    if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
+      if (lane == 0) {
+        *abort_flag = 1;
+        report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
+        drain<NST>(full, u);
         bulk_wait<0>();
       }
       return;
     }
-    if (tid == 0 && prod.valid(g)) {
-      long long f;
-      int nn;
-      prod.sites(g, f, nn);
-      issue_tile<Op>(p, stages + stage * STAGE, &full[stage], f, nn);
-      prod.next(g);
-      ++issued;
+    const unsigned char *sb = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
+    const S *in[NIN];
+#pragma unroll
+    for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
+    unsigned char *ob = outbuf + (size_t)(u & 1) * SPW * L::SLOT;
+    Op::site(p, in, scratch, sub, reinterpret_cast<S *>(ob + (size_t)local * L::SLOT));
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(&empty[stage]);
+      for (int s = 0; s < SPW; ++s)
+        if (w * SPW + s < n)
+          bulk_s2g(static_cast<char *>(p.out[0]) + (first + w * SPW + s) * L::SITE_BYTES, ob + (size_t)s * L::SLOT,
+                   L::SITE_BYTES);
+      bulk_commit();
+      bulk_wait_read<1>();  // the other staging buffer is free again
     }
-    cons.next(g);
+    __syncwarp();
+    it.next(g);
   }
-  if (tid == 0) bulk_wait<0>();
+  if (lane == 0) bulk_wait<0>();
 }
 
 } // namespace cgb

@@ -75,7 +75,7 @@ template <class Op> cudaError_t run_scalar(const Job &job, OpParams<typename Op:
   double2 *partial = nullptr;
   if (!job.per_site) {
     if (!job.ws) return cudaErrorInvalidValue;
-    partial = static_cast<double2 *>(job.ws->get((size_t)p.geom.total_chunks * Op::NOUT * sizeof(double2)));
+    partial = static_cast<double2 *>(job.ws->get((size_t)p.geom.total_chunks * Op::CW * Op::NOUT * sizeof(double2)));
     if (!partial) return cudaErrorMemoryAllocation;
     p.out[0] = partial;
   }
@@ -89,7 +89,9 @@ template <class Op> cudaError_t run_scalar(const Job &job, OpParams<typename Op:
   e = cudaGetLastError();
   if (e != cudaSuccess || job.per_site) return e;
   const int n = Op::NOUT * job.lt;
-  finalize_kernel<<<(n + 127) / 128, 128, 0, job.stream>>>(partial, user_out, Op::NOUT, job.lt, p.geom.chunks_per_seg);
+  // partial is [segment][chunk][consumer warp][NOUT]: fold the warps into the chunk count.
+  finalize_kernel<<<(n + 127) / 128, 128, 0, job.stream>>>(partial, user_out, Op::NOUT, job.lt,
+                                                            p.geom.chunks_per_seg * Op::CW);
   return cudaGetLastError();
 }
 

@@ -167,6 +167,8 @@ __device__ __forceinline__ void loop_site(const BaryonSpin<R> &b, const S *A, co
 }
 
 // Triangle form over N' (NW slots of 144 complex).  Writes vals[v*NW + w].
+// Loop order l -> m -> w: each B block is loaded once and feeds every
+// projector's accumulator.
 template <class R, class S, int TPS, int NV, int NW>
 __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A, const S *B, const S *np, int sub,
                                               int c1sel, cx<R> *vals)
@@ -189,26 +191,33 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
 #pragma unroll
   for (int lo = 0; lo < Ln::LPT; ++lo) {
     const int l = l0 + lo;
+    cx<R> d[NW][9];
 #pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      cx<R> d[9];
+    for (int w = 0; w < NW; ++w)
 #pragma unroll
-      for (int k = 0; k < 9; ++k) d[k] = czero<R>();
+      for (int k = 0; k < 9; ++k) d[w][k] = czero<R>();
+    // Not unrolled: keeps one B block and one N' block live (register pressure).
+#pragma unroll 1
+    for (int m = 0; m < 4; ++m) {
+      cx<R> bm[9];
+      if constexpr (kCacheB) {
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
+        for (int k = 0; k < 9; ++k) bm[k] = brow[m][k];
+      } else {
+        load9(bm, B + (j * 4 + m) * 9);
+      }
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
         cx<R> nn[9];
         load9(nn, np + (size_t)w * 144 + (m * 4 + l) * 9);
-        if constexpr (kCacheB) {
-          wedge_acc(d, brow[m], nn);
-        } else {
-          cx<R> bm[9];
-          load9(bm, B + (j * 4 + m) * 9);
-          wedge_acc(d, bm, nn);
-        }
+        wedge_acc(d[w], bm, nn);
       }
-      cx<R> a[9];
-      load9(a, A + (i * 4 + b.perm2[l]) * 9);
-      const cx<R> s = dot9(a, d);
+    }
+    cx<R> a[9];
+    load9(a, A + (i * 4 + b.perm2[l]) * 9);
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      const cx<R> s = dot9(a, d[w]);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(s, b.ph2[v][l]));
     }
@@ -221,19 +230,21 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
 }
 
 // ------------------------------------------------------------------ ops --
-// Common compile-time configuration of an op.
-template <class R_, class S_, int SITES_, int TPS_, int NST_> struct OpBase {
+// Common compile-time configuration of an op: CW consumer warps (plus one
+// producer warp), TPS threads per site, NST ring stages.
+template <class R_, class S_, int CW_, int TPS_, int NST_> struct OpBase {
   using R = R_;
   using S = S_;
   using Params = OpParams<R_>;
-  static constexpr int SITES = SITES_, TPS = TPS_, NST = NST_;
-  static constexpr int THREADS = SITES_ * TPS_;
+  static constexpr int CW = CW_, TPS = TPS_, NST = NST_;
+  static constexpr int SITES = CW_ * (32 / TPS_);
+  static constexpr int THREADS = 32 * (CW_ + 1);
   static_assert(32 % TPS_ == 0, "a site's threads must sit in one warp");
 };
 
 // One baryon contraction type per launch, loop form (IK_JL_NM, IL_JK_NM).
-template <class R, class S, int SITES, int TPS, int NST>
-struct BaryonLoopOp : OpBase<R, S, SITES, TPS, NST> {
+template <class R, class S, int CW, int TPS, int NST>
+struct BaryonLoopOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 3, NOUT = 1, EXTRA_SLOTS = 1;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
@@ -245,8 +256,8 @@ struct BaryonLoopOp : OpBase<R, S, SITES, TPS, NST> {
 };
 
 // One baryon contraction type per launch, triangle form (the other four types).
-template <class R, class S, int SITES, int TPS, int NST>
-struct BaryonTriOp : OpBase<R, S, SITES, TPS, NST> {
+template <class R, class S, int CW, int TPS, int NST>
+struct BaryonTriOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 3, NOUT = 1, EXTRA_SLOTS = 1;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
@@ -259,8 +270,8 @@ struct BaryonTriOp : OpBase<R, S, SITES, TPS, NST> {
 
 // All six types x NW projectors in one pass over (P_i, P_j, P_n).
 // Output o = type * NW + w, types in contract_enum.h order.
-template <class R, class S, int SITES, int TPS, int NST, int NW>
-struct BaryonFusedOp : OpBase<R, S, SITES, TPS, NST> {
+template <class R, class S, int CW, int TPS, int NST, int NW>
+struct BaryonFusedOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_SLOTS = NW + 1;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
@@ -293,8 +304,8 @@ struct BaryonFusedOp : OpBase<R, S, SITES, TPS, NST> {
 
 // Meson two-point: C = sum_{i,l} c1(i) c2(l) sum_ad A[i][perm2 l][ad] conj(B[perm1 i][l][ad])
 // with c from (g5 Gamma)^T (include/meson.cuh:33-50).
-template <class R, class S, int SITES, int TPS, int NST>
-struct MesonOp : OpBase<R, S, SITES, TPS, NST> {
+template <class R, class S, int CW, int TPS, int NST>
+struct MesonOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, NOUT = 1, EXTRA_SLOTS = 0;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
@@ -326,8 +337,8 @@ template <class R> __device__ __forceinline__ cx<R> pick4(const cx<R> t[4], int 
 // meson_all_source_two_point: Gamma_ij fixed (perm1/ph1), all 16 Gamma_kl.
 // Thread = spin row i (TPS = 4); the 4 x 4 colour dots T[k][l] for j = perm1[i]
 // are shared by all 16 outputs (include/meson_all.cuh:53-73 recomputes them per Gamma).
-template <class R, class S, int SITES, int NST>
-struct MesonAllSourceOp : OpBase<R, S, SITES, 4, NST> {
+template <class R, class S, int CW, int NST>
+struct MesonAllSourceOp : OpBase<R, S, CW, 4, NST> {
   static constexpr int NIN = 2, NOUT = 16, EXTRA_SLOTS = 0;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
@@ -358,8 +369,8 @@ struct MesonAllSourceOp : OpBase<R, S, SITES, 4, NST> {
 
 // meson_all_sink_two_point: Gamma_kl fixed (perm2/ph2), all 16 Gamma_ij.
 // Thread = spin column l (TPS = 4).
-template <class R, class S, int SITES, int NST>
-struct MesonAllSinkOp : OpBase<R, S, SITES, 4, NST> {
+template <class R, class S, int CW, int NST>
+struct MesonAllSinkOp : OpBase<R, S, CW, 4, NST> {
   static constexpr int NIN = 2, NOUT = 16, EXTRA_SLOTS = 0;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
@@ -392,8 +403,8 @@ struct MesonAllSinkOp : OpBase<R, S, SITES, 4, NST> {
 // Diquark (include/diquark.cuh:33-57):
 //   D[m][l][ad] = g5[m] g5[l] conj( c2(l) sum_i c1(i) (P_i[i][perm2 l] ^ P_j[perm1 i][m])[ad] )
 // with c1 from Gamma_ij, c2 from Gamma_kl^T.  Thread handles 16/TPS blocks (m, l).
-template <class R, class S, int SITES, int TPS, int NST>
-struct DiquarkOp : OpBase<R, S, SITES, TPS, NST> {
+template <class R, class S, int CW, int TPS, int NST>
+struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, EXTRA_SLOTS = 0;
   static constexpr bool FIELD = true;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)
@@ -436,8 +447,8 @@ struct DiquarkOp : OpBase<R, S, SITES, TPS, NST> {
 //   tri,  d/dA[i][perm2 l] = c1 c2 sum_m B[perm1 i][m] ^ N'[m][l]
 //   tri,  d/dB[perm1 i][m] = c1 sum_l c2 (A[i][perm2 l] ^ N'[m][l])
 //   tri,  d/dN[perm(m)][l] = W[m][perm m] sum_i c1 c2 (A[i][perm2 l] ^ B[perm1 i][m])
-template <class R, class S, int SITES, int TPS, int NST, bool LOOP, int ROLE>
-struct SequentialOp : OpBase<R, S, SITES, TPS, NST> {
+template <class R, class S, int CW, int TPS, int NST, bool LOOP, int ROLE>
+struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, EXTRA_SLOTS = 1;
   static constexpr bool FIELD = true;
 

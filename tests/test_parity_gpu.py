@@ -9,7 +9,12 @@ from oracle import einsum_oracle as eo
 
 pytestmark = pytest.mark.gpu
 TOL_C128 = 1e-12           # plain form (FP64 throughout)
-TOL_C64_TIMESLICE = 1e-6   # mixed form: max relative error per timeslice vs the FP64 oracle
+# Mixed form (complex64 storage, FP32 arithmetic, FP64 timeslice reduction):
+# |got_t - ref_t| <= 1e-6 * max(|ref_t|, sigma_t), sigma_t = sqrt(sum_{x in t} |ref(x)|^2).
+# On timeslices with a signal (|ref_t| >= sigma_t) this is the plain 1e-6
+# relative bound; with the i.i.d. Gaussian test propagators every timeslice is
+# a zero-mean random walk of site values, and sigma_t is its natural scale.
+TOL_C64_TIMESLICE = 1e-6
 
 LATT = (4, 4, 4, 8)
 
@@ -37,9 +42,11 @@ def cuda(a, c64=False):
     return t.to(torch.complex64) if c64 else t
 
 
-def per_t_rel(got, ref):
+def per_t_rel(got, ref, site):
+    """max_t |got_t - ref_t| / max(|ref_t|, sigma_t) for per-site values `site` [..., V]."""
     got, ref = np.asarray(got), np.asarray(ref)
-    return float(np.max(np.abs(got - ref) / np.abs(ref)))
+    sigma = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, LATT).real)
+    return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), sigma)))
 
 
 def test_ragged_volumes(api, props, c_oracle):
@@ -75,23 +82,25 @@ def test_baryon_all_types_all_gammas_c128(api, props, c_oracle):
 def test_meson_all_per_timeslice(api, props, c_oracle):
     pi, pj, _ = props
     got = api.meson_all_timeslice(cuda(pi), cuda(pj), LATT, 5, source=True).cpu().numpy()
-    ref = eo.timeslice_sum(c_oracle.meson_all_source(pi, pj, 5), LATT)
+    site = c_oracle.meson_all_source(pi, pj, 5)
+    ref = eo.timeslice_sum(site, LATT)
     assert rel_err(got, ref) < TOL_C128
     got64 = api.meson_all_timeslice(cuda(pi, True), cuda(pj, True), LATT, 5, source=True).cpu().numpy()
     for g in range(16):
-        assert per_t_rel(got64[g], ref[g]) < TOL_C64_TIMESLICE, g
+        assert per_t_rel(got64[g], ref[g], site[g]) < TOL_C64_TIMESLICE, g
 
 
 def test_baryon_timeslice_both_precisions(api, props, c_oracle):
     pi, pj, pn = props
     pp = api.projector_plus_minus()
     for t in range(6):
-        ref = eo.timeslice_sum(c_oracle.baryon_general_two_point(pi, pj, pn, t, 5, 5, pp[0]), LATT)
+        site = c_oracle.baryon_general_two_point(pi, pj, pn, t, 5, 5, pp[0])
+        ref = eo.timeslice_sum(site, LATT)
         got = api.baryon(cuda(pi), cuda(pj), cuda(pn), t, 5, 5, project_mn=pp[0], latt=LATT).cpu().numpy()
         assert rel_err(got, ref) < TOL_C128, t
         got64 = api.baryon(cuda(pi, True), cuda(pj, True), cuda(pn, True), t, 5, 5, project_mn=pp[0],
                            latt=LATT).cpu().numpy()
-        assert per_t_rel(got64, ref) < TOL_C64_TIMESLICE, t
+        assert per_t_rel(got64, ref, site) < TOL_C64_TIMESLICE, t
 
 
 def test_fused_all_types(api, props, c_oracle):
@@ -112,7 +121,7 @@ def test_fused_all_types(api, props, c_oracle):
     got64 = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp, latt=LATT).cpu().numpy()
     for t in range(6):
         for w in range(2):
-            assert per_t_rel(got64[t, w], ref[t, w]) < TOL_C64_TIMESLICE, (t, w)
+            assert per_t_rel(got64[t, w], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
 
 
 def test_mixed_field_ops(api, props, c_oracle):
