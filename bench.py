@@ -366,6 +366,67 @@ def run_ours(args, world, rank, local):
     return result
 
 
+PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "loop", "loop128", "meson", "meson128", "meson_all",
+               "diquark", "sequential", "sequential128")
+
+
+def run_profile(args):
+    """One op, nothing else: the command line that ncu captures (small lattice)."""
+    import torch
+
+    from contract_gb300 import _lib, api, build
+    from contract_gb300.lattice import synthetic_propagator
+
+    build.build()
+    lib = _lib.lib()
+    lib.contract_set_error_mode(1)
+    latt = tuple(int(x) for x in args.lattice.split(","))
+    v = latt[0] * latt[1] * latt[2] * latt[3]
+    dev = torch.device("cuda", 0)
+    lib.contract_set_stream(torch.cuda.current_stream(dev).cuda_stream)
+    op = args.profile
+    c64 = not op.endswith("128")
+    base = op[:-3] if op.endswith("128") else op
+    props = [synthetic_propagator(latt, s, m, device=dev) for s, m in ((1, 0.25), (2, 0.25), (3, 0.30))]
+    if c64:
+        props = [api.to_c64(p) for p in props]
+    prec = 1 if c64 else 0
+    latt_c = (ctypes.c_int * 4)(*latt)
+    projs = np.ascontiguousarray(api.projector_plus_minus())
+    out = torch.empty((16, max(v, 1)), dtype=torch.complex128, device=dev)
+    field = torch.empty_like(props[0])
+    a, b_, c = (x.data_ptr() for x in props)
+
+    def step():
+        if base == "fused":
+            lib.contract_baryon_all_types(out.data_ptr(), a, b_, c, v, 5, 5, 2, projs.ctypes.data, prec, latt_c)
+        elif base in ("tri", "loop"):
+            lib.contract_baryon(out.data_ptr(), a, b_, c, 1 if base == "tri" else 0, v, 5, 5, 0,
+                                projs[0].ctypes.data, prec, latt_c)
+        elif base == "meson":
+            lib.contract_meson(out.data_ptr(), a, b_, v, 15, 15, prec, latt_c)
+        elif base == "meson_all":
+            ptrs = (ctypes.c_void_p * 16)(*[out[k].data_ptr() for k in range(16)])
+            lib.contract_meson_all(ptrs, a, b_, v, 5, 1, prec, latt_c)
+        elif base == "diquark":
+            lib.contract_diquark(field.data_ptr(), a, b_, v, 5, 5, prec)
+        elif base == "sequential":
+            lib.contract_sequential(a, b_, c, 1, 2, v, 5, 5, 8, prec)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    e1.synchronize()
+    if lib.contract_last_error():
+        raise RuntimeError(lib.contract_last_error_message().decode())
+    print(json.dumps({"profile": op, "lattice": list(latt), "ms_per_launch": e0.elapsed_time(e1) / args.steps}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -374,7 +435,12 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--cpu-slices", type=int, default=8, help="timeslices in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", choices=PROFILE_OPS, help="run only this op (for ncu captures)")
+    ap.add_argument("--lattice", default="24,24,24,16", help="Lx,Ly,Lz,Lt for --profile")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     world, rank, local = dist_setup(args)
     try:
         if args.impl == "reference":

@@ -235,6 +235,52 @@ void fill_proj(cgb::ProjOperand<double> &w, int gamma_mn, const double *project_
   w.is_perm = perm ? 1 : 0;
 }
 
+// Write the projectors W_w (w < nw, each 16 complex row-major, or Gamma(gamma_mn)
+// when `projs` is null) in the gamma basis: W = sum_g c_g Gamma(g) with
+// c_g = Tr(Gamma(g)^dagger W) / 4 = (1/4) sum_m i^(-ph_g(m)) W[m][perm_g(m)].
+void fill_clifford(cgb::CliffordSet<double> &cl, const double *const *projs, int nw, int gamma_mn)
+{
+  cl = {};
+  static const double re[4] = {1, 0, -1, 0}, im[4] = {0, 1, 0, -1};
+  double c[2][16][2] = {};
+  bool used[16] = {};
+  for (int w = 0; w < nw; ++w) {
+    if (!projs) {
+      c[w][gamma_mn][0] = 1.0;
+      used[gamma_mn] = true;
+      continue;
+    }
+    for (int g = 0; g < 16; ++g) {
+      const cgb::SignedPerm sp = cgb::sp_gamma(g);
+      double x = 0, y = 0;
+      for (int m = 0; m < 4; ++m) {
+        const double *wv = projs[w] + 2 * (m * 4 + sp.perm[m]);
+        // multiply by conj(i^ph) = i^(-ph)
+        const double cr = re[sp.ph[m]], ci = -im[sp.ph[m]];
+        x += cr * wv[0] - ci * wv[1];
+        y += cr * wv[1] + ci * wv[0];
+      }
+      c[w][g][0] = x / 4;
+      c[w][g][1] = y / 4;
+      if (x != 0.0 || y != 0.0) used[g] = true;
+    }
+  }
+  for (int g = 0; g < 16; ++g) {
+    if (!used[g]) continue;
+    const int k = cl.ng++;
+    const cgb::SignedPerm sp = cgb::sp_gamma(g);
+    for (int m = 0; m < 4; ++m) {
+      cl.perm[k][m] = (uint8_t)sp.perm[m];
+      cl.ph[k][m] = (uint8_t)sp.ph[m];
+      if (sp.ph[m]) cl.has_phase[k] = 1;
+    }
+    for (int w = 0; w < nw; ++w) {
+      cl.coef[w][k][0] = c[w][g][0];
+      cl.coef[w][k][1] = c[w][g][1];
+    }
+  }
+}
+
 // Contraction type -> canonical form (see ops.cuh): loop or triangle, whether
 // P_i and P_j swap roles, and the c1/c2 phase rows.
 struct TypeForm {
@@ -333,6 +379,7 @@ void do_baryon(void *correl, const void *pi, const void *pj, const void *pn, int
   set_row(p.b.ph1[0], f.c1);
   set_row(p.b.ph2[0], f.c2);
   fill_proj(p.b.proj[0], gmn, proj);
+  fill_clifford(p.b.cl, proj ? &proj : nullptr, 1, gmn);
   cuda_ok(cgb::launch_baryon(job, f.loop, p), proj ? "baryon_general_two_point" : "baryon_two_point");
 }
 
@@ -597,7 +644,9 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
   set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);  // IK_JL_NM, IK_JM_NL, IM_JK_NL
   set_row(p.b.ph2[1], kG.ph[gamma_kl]);    // IL_JK_NM, IL_JM_NK, IM_JL_NK
   const double *pr = static_cast<const double *>(projectors);
-  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pr + 32 * w);
+  const double *pw[2] = {pr, pr + 32};
+  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
+  fill_clifford(p.b.cl, pw, nproj, 0);
   cuda_ok(cgb::launch_baryon_fused(job, nproj, p), "contract_baryon_all_types");
 }
 

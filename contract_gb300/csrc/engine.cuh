@@ -91,7 +91,7 @@ template <class S> struct SiteLayout {
 // Shared-memory map of an engine kernel:
 //   [0, 128)        full[NST], empty[NST] mbarriers, abort flag
 //   stages          NST x NIN x SITES slots
-//   extra           SITES x EXTRA_SLOTS slots (per-site op scratch)
+//   extra           SITES x EXTRA_BYTES (per-site op scratch)
 //   tail            scalar ops: per-warp site values [CW][SPW][NOUT] (cx<R>)
 //                   field ops:  per-warp output staging [CW][2][SPW] slots
 template <class Op> struct Smem {
@@ -99,7 +99,7 @@ template <class Op> struct Smem {
   static constexpr size_t STAGE = (size_t)Op::NIN * Op::SITES * L::SLOT;
   static constexpr size_t STAGES = 128;
   static constexpr size_t EXTRA = STAGES + Op::NST * STAGE;
-  static constexpr size_t TAIL = EXTRA + (size_t)Op::EXTRA_SLOTS * Op::SITES * L::SLOT;
+  static constexpr size_t TAIL = EXTRA + (size_t)Op::EXTRA_BYTES * Op::SITES;
   static constexpr size_t tail_bytes()
   {
     if constexpr (Op::FIELD) return 2ull * Op::SITES * L::SLOT;
@@ -110,6 +110,46 @@ template <class Op> struct Smem {
 };
 
 template <class Op> constexpr size_t engine_smem_bytes() { return Smem<Op>::BYTES; }
+
+// FP32 ops ask for two CTAs per SM when their shared memory fits (228 KB per
+// SM, 1 KB reserved per CTA), which caps registers at 128 per thread; FP64 ops
+// are bound by the FP64 pipe and keep one CTA with the full register file.
+template <class Op> constexpr int min_blocks()
+{
+  return (sizeof(typename Op::R) == 4 && 2 * (Smem<Op>::BYTES + 1024) <= 233472) ? 2 : 1;
+}
+
+// Running sum in the op's precision.  FP32 uses a compensated (two-sum)
+// accumulator so that chunk sums lose nothing before they reach FP64; FP64 is
+// a plain sum.
+template <class R> struct ChunkSum;
+template <> struct ChunkSum<float> {
+  float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
+  __device__ __forceinline__ static void two_sum(float &h, float &l, float v)
+  {
+    const float s = h + v;
+    const float bp = s - h;
+    l += (h - (s - bp)) + (v - bp);
+    h = s;
+  }
+  __device__ __forceinline__ void add(cx<float> v)
+  {
+    two_sum(hx, lx, v.x);
+    two_sum(hy, ly, v.y);
+  }
+  __device__ __forceinline__ double2 value() const { return make_double2((double)hx + (double)lx, (double)hy + (double)ly); }
+  __device__ __forceinline__ void reset() { hx = lx = hy = ly = 0.f; }
+};
+template <> struct ChunkSum<double> {
+  double x = 0.0, y = 0.0;
+  __device__ __forceinline__ void add(cx<double> v)
+  {
+    x += v.x;
+    y += v.y;
+  }
+  __device__ __forceinline__ double2 value() const { return make_double2(x, y); }
+  __device__ __forceinline__ void reset() { x = y = 0.0; }
+};
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
@@ -164,7 +204,7 @@ template <int NST> __device__ void drain(uint64_t *full, int from)
 
 // ------------------------------------------------------------ scalar ops --
 template <class Op>
-__global__ void __launch_bounds__(Op::THREADS, 1) scalar_kernel(const __grid_constant__ typename Op::Params p)
+__global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) scalar_kernel(const __grid_constant__ typename Op::Params p)
 {
   using S = typename Op::S;
   using R = typename Op::R;
@@ -196,8 +236,8 @@ __global__ void __launch_bounds__(Op::THREADS, 1) scalar_kernel(const __grid_con
   const int local = lane / TPS, sub = lane % TPS;
   const int site = w * SPW + local;
   cx<R> *sv = reinterpret_cast<cx<R> *>(smem + Smem<Op>::TAIL) + (size_t)w * SPW * NOUT;  // [SPW][NOUT]
-  S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_SLOTS * L::SLOT);
-  double2 chunk_acc = make_double2(0.0, 0.0);  // lane o < NOUT: output o
+  S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_BYTES);
+  ChunkSum<R> chunk_acc;  // lane o < NOUT: output o
 
   TileIter<SITES> it;
   it.set_chunk(g, blockIdx.x);
@@ -239,14 +279,11 @@ __global__ void __launch_bounds__(Op::THREADS, 1) scalar_kernel(const __grid_con
       }
       __syncwarp();
       if (lane < NOUT) {
-        cx<R> t = sv[lane];
 #pragma unroll
-        for (int s = 1; s < SPW; ++s) t = cadd(t, sv[s * NOUT + lane]);
-        chunk_acc.x += double(t.x);
-        chunk_acc.y += double(t.y);
+        for (int s = 0; s < SPW; ++s) chunk_acc.add(sv[s * NOUT + lane]);
         if (it.last_in_chunk()) {
-          static_cast<double2 *>(p.out[0])[((size_t)it.chunk * CW + w) * NOUT + lane] = chunk_acc;
-          chunk_acc = make_double2(0.0, 0.0);
+          static_cast<double2 *>(p.out[0])[((size_t)it.chunk * CW + w) * NOUT + lane] = chunk_acc.value();
+          chunk_acc.reset();
         }
       }
       __syncwarp();
@@ -257,7 +294,7 @@ __global__ void __launch_bounds__(Op::THREADS, 1) scalar_kernel(const __grid_con
 
 // ------------------------------------------------------------- field ops --
 template <class Op>
-__global__ void __launch_bounds__(Op::THREADS, 1) field_kernel(const __grid_constant__ typename Op::Params p)
+__global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(const __grid_constant__ typename Op::Params p)
 {
   using S = typename Op::S;
   using L = SiteLayout<S>;
@@ -287,7 +324,7 @@ __global__ void __launch_bounds__(Op::THREADS, 1) field_kernel(const __grid_cons
   const int w = warp - 1;
   const int local = lane / TPS, sub = lane % TPS;
   const int site = w * SPW + local;
-  S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_SLOTS * L::SLOT);
+  S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_BYTES);
   unsigned char *outbuf = smem + Smem<Op>::TAIL + (size_t)w * 2 * SPW * L::SLOT;  // [2][SPW] slots
 
   TileIter<SITES> it;

@@ -76,6 +76,18 @@ template <class R> OpParams<R> convert_params(const OpParams<double> &p)
     }
     d.is_perm = s.is_perm;
   }
+  o.b.cl.ng = p.b.cl.ng;
+  for (int k = 0; k < 16; ++k) {
+    o.b.cl.has_phase[k] = p.b.cl.has_phase[k];
+    for (int r = 0; r < 4; ++r) {
+      o.b.cl.perm[k][r] = p.b.cl.perm[k][r];
+      o.b.cl.ph[k][r] = p.b.cl.ph[k][r];
+    }
+    for (int w = 0; w < 2; ++w) {
+      o.b.cl.coef[w][k][0] = R(p.b.cl.coef[w][k][0]);
+      o.b.cl.coef[w][k][1] = R(p.b.cl.coef[w][k][1]);
+    }
+  }
   return o;
 }
 

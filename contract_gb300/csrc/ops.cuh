@@ -43,11 +43,23 @@ template <class R> struct ProjOperand {
   int is_perm;
 };
 
+// Up to two projectors written in the gamma basis, W_w = sum_k coef[w][k] Gamma(g_k):
+// N'_w[m][l] = sum_k coef[w][k] i^ph[k][m] N[perm[k][m]][l], so the triangle
+// form needs one spin-permuted pass over N per basis term and no N' buffer.
+template <class R> struct CliffordSet {
+  int ng;
+  uint8_t perm[16][4];
+  uint8_t ph[16][4];
+  uint8_t has_phase[16];
+  R coef[2][16][2];
+};
+
 template <class R> struct BaryonSpin {
   uint8_t perm1[4], perm2[4];
   uint8_t ph1[2][4];  // [0]: c1 for A = P_i groups, [1]: c1 for the swapped (IM_*) group
   uint8_t ph2[2][4];  // c2 variants (one per output of a loop/tri evaluation)
   ProjOperand<R> proj[2];
+  CliffordSet<R> cl;
 };
 
 template <class R> struct MesonSpin {
@@ -229,6 +241,57 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
     for (int w = 0; w < NW; ++w) vals[v * NW + w] = mul_phase(acc[v][w], p1);
 }
 
+// Triangle form with the projectors in the gamma basis (CliffordSet):
+//   D_k = sum_m i^ph[k][m] B[perm1 i][m] ^ N[perm[k][m]][l],  s_k = A[i][perm2 l] . D_k
+//   vals[v*NW + w] = c1(i) sum_l c2_v(l) sum_k coef[w][k] s_k
+template <class R, class S, int TPS, int NV, int NW>
+__device__ __forceinline__ void triangle_cliff_site(const BaryonSpin<R> &b, const S *A, const S *B, const S *N, int sub,
+                                                    int c1sel, cx<R> *vals)
+{
+  using Ln = Lanes<TPS>;
+  const CliffordSet<R> &cl = b.cl;
+  const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT;
+  const int j = b.perm1[i];
+  cx<R> acc[NV][NW];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int w = 0; w < NW; ++w) acc[v][w] = czero<R>();
+#pragma unroll
+  for (int lo = 0; lo < Ln::LPT; ++lo) {
+    const int l = l0 + lo;
+    cx<R> a[9];
+    load9(a, A + (i * 4 + b.perm2[l]) * 9);
+#pragma unroll 1
+    for (int k = 0; k < cl.ng; ++k) {
+      cx<R> d[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) d[e] = czero<R>();
+      const bool phased = cl.has_phase[k];
+#pragma unroll 1
+      for (int m = 0; m < 4; ++m) {
+        cx<R> bm[9], nn[9];
+        load9(bm, B + (j * 4 + m) * 9);
+        load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
+        if (phased) phase9(bm, cl.ph[k][m]);
+        wedge_acc(d, bm, nn);
+      }
+      const cx<R> s = dot9(a, d);
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        const cx<R> t = cmul(cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(t, b.ph2[v][l]));
+      }
+    }
+  }
+  const uint32_t p1 = b.ph1[c1sel][i];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int w = 0; w < NW; ++w) vals[v * NW + w] = mul_phase(acc[v][w], p1);
+}
+
 // ------------------------------------------------------------------ ops --
 // Common compile-time configuration of an op: CW consumer warps (plus one
 // producer warp), TPS threads per site, NST ring stages.
@@ -242,10 +305,13 @@ template <class R_, class S_, int CW_, int TPS_, int NST_> struct OpBase {
   static_assert(32 % TPS_ == 0, "a site's threads must sit in one warp");
 };
 
+// Bytes of n complex values of storage type S, rounded up to 16.
+template <class S> constexpr int cbytes(int n) { return (int)((n * sizeof(S) + 15) / 16 * 16); }
+
 // One baryon contraction type per launch, loop form (IK_JL_NM, IL_JK_NM).
 template <class R, class S, int CW, int TPS, int NST>
 struct BaryonLoopOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 3, NOUT = 1, EXTRA_SLOTS = 1;
+  static constexpr int NIN = 3, NOUT = 1, EXTRA_BYTES = cbytes<S>(9);
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
@@ -255,10 +321,11 @@ struct BaryonLoopOp : OpBase<R, S, CW, TPS, NST> {
   }
 };
 
-// One baryon contraction type per launch, triangle form (the other four types).
+// One baryon contraction type per launch, triangle form (the other four
+// types), with N' = W N materialised per site (any 4x4 projector).
 template <class R, class S, int CW, int TPS, int NST>
 struct BaryonTriOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 3, NOUT = 1, EXTRA_SLOTS = 1;
+  static constexpr int NIN = 3, NOUT = 1, EXTRA_BYTES = cbytes<S>(144) + 16;  // +16: bank stagger
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
@@ -268,15 +335,60 @@ struct BaryonTriOp : OpBase<R, S, CW, TPS, NST> {
   }
 };
 
-// All six types x NW projectors in one pass over (P_i, P_j, P_n).
+// Triangle form, one type per launch, with W a combination of few gamma
+// matrices (always one for baryon_two_point): no N' buffer.
+template <class R, class S, int CW, int TPS, int NST>
+struct BaryonTriCliffOp : OpBase<R, S, CW, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 1, EXTRA_BYTES = 0;
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
+  {
+    triangle_cliff_site<R, S, TPS, 1, 1>(p.b, in[0], in[1], in[2], sub, 0, vals);
+  }
+};
+
+// All six types x NW projectors in one pass over (P_i, P_j, P_n), projectors
+// in the gamma basis (e.g. (1 +- g4)/2 = (Gamma(0) +- Gamma(8))/2).
 // Output o = type * NW + w, types in contract_enum.h order.
 template <class R, class S, int CW, int TPS, int NST, int NW>
-struct BaryonFusedOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_SLOTS = NW + 1;
+struct BaryonFusedCliffOp : OpBase<R, S, CW, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW);
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
-    S *q = scratch + (size_t)NW * 144;
+    build_q<R, S, TPS, NW>(p.b, in[2], scratch, sub);
+    __syncwarp();
+    cx<R> t[2 * NW];
+    loop_site<R, S, TPS, 2, NW>(p.b, in[0], in[1], scratch, sub, 0, t);  // IK_JL_NM, IL_JK_NM
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      vals[0 * NW + w] = t[0 * NW + w];
+      vals[2 * NW + w] = t[1 * NW + w];
+    }
+    triangle_cliff_site<R, S, TPS, 2, NW>(p.b, in[0], in[1], in[2], sub, 0, t);  // IK_JM_NL, IL_JM_NK
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      vals[1 * NW + w] = t[0 * NW + w];
+      vals[3 * NW + w] = t[1 * NW + w];
+    }
+    triangle_cliff_site<R, S, TPS, 2, NW>(p.b, in[1], in[0], in[2], sub, 1, t);  // IM_JK_NL, IM_JL_NK
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      vals[4 * NW + w] = t[0 * NW + w];
+      vals[5 * NW + w] = t[1 * NW + w];
+    }
+  }
+};
+
+// All six types x NW projectors with N'_w = W_w N materialised per site
+// (projectors that are not short gamma-basis combinations).
+template <class R, class S, int CW, int TPS, int NST, int NW>
+struct BaryonFusedOp : OpBase<R, S, CW, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(144) * NW + cbytes<S>(9 * NW);
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    S *q = reinterpret_cast<S *>(reinterpret_cast<char *>(scratch) + cbytes<S>(144) * NW);
     build_nprime<R, S, TPS, NW>(p.b, in[2], scratch, sub);
     build_q<R, S, TPS, NW>(p.b, in[2], q, sub);
     __syncwarp();
@@ -306,7 +418,7 @@ struct BaryonFusedOp : OpBase<R, S, CW, TPS, NST> {
 // with c from (g5 Gamma)^T (include/meson.cuh:33-50).
 template <class R, class S, int CW, int TPS, int NST>
 struct MesonOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 2, NOUT = 1, EXTRA_SLOTS = 0;
+  static constexpr int NIN = 2, NOUT = 1, EXTRA_BYTES = 0;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
   {
@@ -339,7 +451,7 @@ template <class R> __device__ __forceinline__ cx<R> pick4(const cx<R> t[4], int 
 // are shared by all 16 outputs (include/meson_all.cuh:53-73 recomputes them per Gamma).
 template <class R, class S, int CW, int NST>
 struct MesonAllSourceOp : OpBase<R, S, CW, 4, NST> {
-  static constexpr int NIN = 2, NOUT = 16, EXTRA_SLOTS = 0;
+  static constexpr int NIN = 2, NOUT = 16, EXTRA_BYTES = 0;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
   {
@@ -371,7 +483,7 @@ struct MesonAllSourceOp : OpBase<R, S, CW, 4, NST> {
 // Thread = spin column l (TPS = 4).
 template <class R, class S, int CW, int NST>
 struct MesonAllSinkOp : OpBase<R, S, CW, 4, NST> {
-  static constexpr int NIN = 2, NOUT = 16, EXTRA_SLOTS = 0;
+  static constexpr int NIN = 2, NOUT = 16, EXTRA_BYTES = 0;
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, cx<R> *vals)
   {
@@ -405,7 +517,7 @@ struct MesonAllSinkOp : OpBase<R, S, CW, 4, NST> {
 // with c1 from Gamma_ij, c2 from Gamma_kl^T.  Thread handles 16/TPS blocks (m, l).
 template <class R, class S, int CW, int TPS, int NST>
 struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 2, EXTRA_SLOTS = 0;
+  static constexpr int NIN = 2, EXTRA_BYTES = 0;
   static constexpr bool FIELD = true;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)
   {
@@ -449,7 +561,7 @@ struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
 //   tri,  d/dN[perm(m)][l] = W[m][perm m] sum_i c1 c2 (A[i][perm2 l] ^ B[perm1 i][m])
 template <class R, class S, int CW, int TPS, int NST, bool LOOP, int ROLE>
 struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 2, EXTRA_SLOTS = 1;
+  static constexpr int NIN = 2, EXTRA_BYTES = cbytes<S>(144) + 16;
   static constexpr bool FIELD = true;
 
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, S *out)
