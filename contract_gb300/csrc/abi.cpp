@@ -133,6 +133,19 @@ struct DeviceWorkspace : cgb::Workspace {
   }
 };
 
+// Hands out the library's fixed static scratch array; never allocates.  A
+// request larger than the array is remembered and refused.
+struct StaticWorkspace : cgb::Workspace {
+  void *base = nullptr;
+  size_t cap = 0;
+  size_t requested = 0;
+  void *get(size_t bytes) override
+  {
+    requested = bytes;
+    return bytes <= cap ? base : nullptr;
+  }
+};
+
 bool gamma_ok(int g, const char *name)
 {
   if (g >= 0 && g < 16) return true;
@@ -648,6 +661,59 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
   for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
   fill_clifford(p.b.cl, pw, nproj, 0);
   cuda_ok(cgb::launch_baryon_fused(job, nproj, p), "contract_baryon_all_types");
+}
+
+int contract_baryon_all_types_noalloc(void *correl, const void *propag_i, const void *propag_j,
+                                      const void *propag_n, size_t volume, int gamma_ij, int gamma_kl, int nproj,
+                                      const void *projectors, int precision, const int *lattice)
+{
+  if (!lattice) {
+    invalid("contract_baryon_all_types_noalloc needs a lattice (per-site output needs no scratch: "
+            "use contract_baryon_all_types)");
+    return CONTRACT_ERROR_INVALID_ARGUMENT;
+  }
+  if (nproj < 1 || nproj > 2) {
+    invalid("nproj must be 1 or 2 (got %d)", nproj);
+    return CONTRACT_ERROR_INVALID_ARGUMENT;
+  }
+  if (!projectors) {
+    invalid("projectors is NULL");
+    return CONTRACT_ERROR_INVALID_ARGUMENT;
+  }
+  if (!gamma_ok(gamma_ij, "gamma_ij") || !gamma_ok(gamma_kl, "gamma_kl") || !prec_ok(precision) ||
+      !ptr_ok(correl, volume, "correl") || !ptr_ok(propag_i, volume, "propag_i") ||
+      !ptr_ok(propag_j, volume, "propag_j") || !ptr_ok(propag_n, volume, "propag_n"))
+    return CONTRACT_ERROR_INVALID_ARGUMENT;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, precision, volume, lattice, &s)) return contract_last_error();
+  StaticWorkspace ws;
+  if (!cuda_ok(cgb::static_scratch(&ws.base, &ws.cap), "static scratch address")) return contract_last_error();
+  job.ws = &ws;
+  OpParams<double> p {};
+  p.in[0] = propag_i;
+  p.in[1] = propag_j;
+  p.in[2] = propag_n;
+  for (int o = 0; o < 6 * nproj; ++o) p.out[o] = static_cast<char *>(correl) + o * (size_t)lattice[3] * 16;
+  set_row(p.b.perm1, kG.perm[gamma_ij]);
+  set_row(p.b.perm2, kG.perm[gamma_kl]);
+  set_row(p.b.ph1[0], kG.ph[gamma_ij]);
+  set_row(p.b.ph1[1], kG.ph_t[gamma_ij]);
+  set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);
+  set_row(p.b.ph2[1], kG.ph[gamma_kl]);
+  const double *pr = static_cast<const double *>(projectors);
+  const double *pw[2] = {pr, pr + 32};
+  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
+  fill_clifford(p.b.cl, pw, nproj, 0);
+  const cudaError_t e = cgb::launch_baryon_fused(job, nproj, p);
+  if (e != cudaSuccess && ws.requested > ws.cap) {
+    invalid("lattice {%d, %d, %d, %d} needs %zu bytes of partial sums, more than the %zu-byte static scratch of "
+            "contract_baryon_all_types_noalloc (use contract_baryon_all_types)",
+            lattice[0], lattice[1], lattice[2], lattice[3], ws.requested, ws.cap);
+    return CONTRACT_ERROR_INVALID_ARGUMENT;
+  }
+  if (!cuda_ok(e, "contract_baryon_all_types_noalloc")) return contract_last_error();
+  return CONTRACT_SUCCESS;
 }
 
 void contract_diquark(void *diquark, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,

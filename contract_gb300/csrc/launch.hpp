@@ -42,6 +42,9 @@ cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParam
 cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64);
 // Address of this device's status word (a __device__ variable of the library).
 cudaError_t device_status_ptr(DeviceStatus **out);
+// Device address and size of the fixed scratch array used by the
+// allocation-free entry point (noalloc.cu).
+cudaError_t static_scratch(void **ptr, size_t *bytes);
 
 // ---- helpers shared by the launcher TUs --------------------------------------
 template <class R> OpParams<R> convert_params(const OpParams<double> &p)

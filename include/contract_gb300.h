@@ -107,6 +107,28 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
                                size_t volume, int gamma_ij, int gamma_kl, int nproj, const void *projectors,
                                int precision, const int *lattice);
 
+/* contract_baryon_all_types with a non-NULL lattice, for callers that cannot
+ * let the library allocate device memory (a pool allocator in the host
+ * framework owns the free memory, cudaMalloc's implicit synchronisation is
+ * not acceptable, or the host requires an allocation-free library as the
+ * reference library is).  No counterpart in the reference.
+ *
+ * The per-timeslice partial sums go into a fixed 16 MiB static device array
+ * that every GPU loading the library holds until exit; nothing is allocated
+ * or freed.  The array is fully overwritten by each call (nothing needs to
+ * start at zero), and all calls share it: calls that overlap on the GPU (on
+ * different streams, or in different host threads) race.  The first call on
+ * a device looks up the array's device address; make it before any stream
+ * capture.  A lattice whose partial sums do not fit the array is rejected
+ * with CONTRACT_ERROR_INVALID_ARGUMENT and a message naming both sizes (each
+ * of the 2 Lt half-timeslices needs at least 1344 bytes with two projectors,
+ * so Lt beyond about 6000 never fits; a 48^3 x 96 lattice does).  Returns
+ * CONTRACT_SUCCESS or the error code (errors also follow the error mode, like
+ * every other call). */
+int contract_baryon_all_types_noalloc(void *correl, const void *propag_i, const void *propag_j,
+                                      const void *propag_n, size_t volume, int gamma_ij, int gamma_kl, int nproj,
+                                      const void *projectors, int precision, const int *lattice);
+
 /* baryon_diquark / baryon_sequential_two_point with a storage precision
  * (fields are read and written in that precision). */
 void contract_diquark(void *diquark, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
