@@ -216,6 +216,7 @@ def run_ours(args, world, rank, local):
     build.build()
     lib = _lib.lib()
     lib.contract_set_error_mode(1)
+    lib.contract_set_autotune(0 if args.no_autotune else 1)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     lib.contract_set_stream(stream.cuda_stream)
@@ -359,6 +360,7 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": world * units / (ms_e2e * 1e-3) / 1e9, "unit": "GSite/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
             "gpu_launches": 2 * args.steps,
+            "autotune": autotune_report(lib),
             "clocks": clocks.summary(),
             "cpu_baseline": None if cb is None else {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
         }
@@ -366,8 +368,14 @@ def run_ours(args, world, rank, local):
     return result
 
 
-PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "loop", "loop128", "meson", "meson128", "meson_all",
+PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "meson", "meson128", "meson_all",
                "diquark", "sequential", "sequential128")
+
+
+def autotune_report(lib):
+    buf = ctypes.create_string_buffer(8192)
+    lib.contract_autotune_report(buf, len(buf))
+    return [line.split("\t") for line in buf.value.decode().splitlines()]
 
 
 def run_profile(args):
@@ -380,6 +388,7 @@ def run_profile(args):
     build.build()
     lib = _lib.lib()
     lib.contract_set_error_mode(1)
+    lib.contract_set_autotune(0 if args.no_autotune else 1)
     latt = tuple(int(x) for x in args.lattice.split(","))
     v = latt[0] * latt[1] * latt[2] * latt[3]
     dev = torch.device("cuda", 0)
@@ -400,9 +409,10 @@ def run_profile(args):
     def step():
         if base == "fused":
             lib.contract_baryon_all_types(out.data_ptr(), a, b_, c, v, 5, 5, 2, projs.ctypes.data, prec, latt_c)
-        elif base in ("tri", "loop"):
-            lib.contract_baryon(out.data_ptr(), a, b_, c, 1 if base == "tri" else 0, v, 5, 5, 0,
-                                projs[0].ctypes.data, prec, latt_c)
+        elif base in ("tri", "loop"):  # baryon_two_point form: Gamma_mn = g4
+            lib.contract_baryon(out.data_ptr(), a, b_, c, 1 if base == "tri" else 0, v, 5, 5, 8, None, prec, latt_c)
+        elif base == "trigen":  # general projector (1 + g4)/2
+            lib.contract_baryon(out.data_ptr(), a, b_, c, 1, v, 5, 5, 0, projs[0].ctypes.data, prec, latt_c)
         elif base == "meson":
             lib.contract_meson(out.data_ptr(), a, b_, v, 15, 15, prec, latt_c)
         elif base == "meson_all":
@@ -424,7 +434,8 @@ def run_profile(args):
     e1.synchronize()
     if lib.contract_last_error():
         raise RuntimeError(lib.contract_last_error_message().decode())
-    print(json.dumps({"profile": op, "lattice": list(latt), "ms_per_launch": e0.elapsed_time(e1) / args.steps}))
+    print(json.dumps({"profile": op, "lattice": list(latt), "ms_per_launch": e0.elapsed_time(e1) / args.steps,
+                      "autotune": autotune_report(lib)}))
 
 
 def main():
@@ -435,6 +446,7 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--cpu-slices", type=int, default=8, help="timeslices in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-autotune", action="store_true", help="use the default tile shapes")
     ap.add_argument("--profile", choices=PROFILE_OPS, help="run only this op (for ncu captures)")
     ap.add_argument("--lattice", default="24,24,24,16", help="Lx,Ly,Lz,Lt for --profile")
     args = ap.parse_args()

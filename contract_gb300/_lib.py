@@ -43,6 +43,8 @@ SIGNATURES = {
     "contract_check_device": (c_int, []),
     "contract_set_stream": (None, [c_void_p]),
     "contract_get_stream": (c_void_p, []),
+    "contract_set_autotune": (None, [c_int]),
+    "contract_autotune_report": (c_int, [c_void_p, c_size_t]),
     "contract_workspace_reserve": (c_int, [c_size_t]),
     "contract_workspace_bytes": (c_size_t, [c_int_p, c_int]),
     "contract_gamma_table": (None, [c_int_p, c_int_p]),

@@ -12,7 +12,11 @@
 #include <cstdlib>
 #include <cstdint>
 #include <cstring>
+#include <cmath>
+#include <fstream>
+#include <map>
 #include <mutex>
+#include <sstream>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -145,6 +149,126 @@ struct StaticWorkspace : cgb::Workspace {
     return bytes <= cap ? base : nullptr;
   }
 };
+
+// ------------------------------------------------------------- autotuner --
+// Ops with several compiled tile shapes (Kind in launch.hpp) are tuned per
+// (op, precision, projector count, lattice shape): the first call with a new
+// key times every variant on the call's own data (one warm-up launch, then two
+// timed launches each, CUDA events on the library's stream), keeps the fastest
+// and re-launches it so the output is that variant's.  Choices live in memory
+// and, when CONTRACT_TUNE_CACHE names a file, are appended there and read
+// back by later processes.  Tuning is off unless CONTRACT_AUTOTUNE=1 or
+// contract_set_autotune(1); it never runs during stream capture.  Untuned
+// calls use each launcher's default variant.
+struct TuneEntry {
+  int variant;
+  float ms;
+  std::string name;
+};
+
+struct Tuner {
+  std::mutex mu;
+  std::map<std::string, TuneEntry> choice;
+  int enabled = -1;
+  bool loaded = false;
+  std::string path;
+};
+Tuner g_tune;
+
+bool autotune_enabled()
+{
+  if (g_tune.enabled < 0) {
+    const char *e = std::getenv("CONTRACT_AUTOTUNE");
+    g_tune.enabled = (e && e[0] == '1') ? 1 : 0;
+  }
+  return g_tune.enabled == 1;
+}
+
+std::string tune_key(cgb::Kind kind, const cgb::Job &job, int aux)
+{
+  std::ostringstream k;
+  k << "kind=" << (int)kind << ",prec=" << (int)job.prec << ",aux=" << aux << ",volume=" << job.volume
+    << ",lt=" << (job.per_site ? 0 : job.lt) << ",half=" << job.half_slice;
+  return k.str();
+}
+
+// Caller holds g_tune.mu.
+void tune_load_locked()
+{
+  if (g_tune.loaded) return;
+  g_tune.loaded = true;
+  const char *p = std::getenv("CONTRACT_TUNE_CACHE");
+  if (!p || !*p) return;
+  g_tune.path = p;
+  std::ifstream f(g_tune.path);
+  std::string line;
+  while (std::getline(f, line)) {
+    std::istringstream ls(line);
+    std::string key, name;
+    int v = -1;
+    float ms = 0;
+    if (std::getline(ls, key, '\t') && (ls >> v >> name >> ms)) g_tune.choice[key] = {v, ms, name};
+  }
+}
+
+bool stream_capturing(cudaStream_t s)
+{
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &st) != cudaSuccess) return true;
+  return st != cudaStreamCaptureStatusNone;
+}
+
+template <class Launch> cudaError_t tuned_launch(cgb::Kind kind, cgb::Job job, int aux, Launch launch)
+{
+  const char *const *names = nullptr;
+  const int n = cgb::launch_variants(kind, job.prec, aux, &names);
+  if (n <= 1 || job.volume == 0) return launch(job);
+  const std::string key = tune_key(kind, job, aux);
+  int v = -1;
+  {
+    std::lock_guard<std::mutex> lk(g_tune.mu);
+    tune_load_locked();
+    auto it = g_tune.choice.find(key);
+    if (it != g_tune.choice.end() && it->second.variant < n && it->second.name == names[it->second.variant])
+      v = it->second.variant;
+  }
+  if (v < 0 && autotune_enabled() && !stream_capturing(job.stream)) {
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return cudaGetLastError();
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      return cudaGetLastError();
+    }
+    float best = INFINITY;
+    for (int c = 0; c < n; ++c) {
+      job.variant = c;
+      if (launch(job) != cudaSuccess) continue;
+      cudaEventRecord(e0, job.stream);
+      cudaError_t e = launch(job);
+      if (e == cudaSuccess) e = launch(job);
+      cudaEventRecord(e1, job.stream);
+      if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) continue;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms / 2 < best) {
+        best = ms / 2;
+        v = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (v >= 0) {
+      std::lock_guard<std::mutex> lk(g_tune.mu);
+      g_tune.choice[key] = {v, best, names[v]};
+      if (!g_tune.path.empty()) {
+        std::ofstream f(g_tune.path, std::ios::app);
+        f << key << '\t' << v << ' ' << names[v] << ' ' << best << '\n';
+      }
+    }
+  }
+  job.variant = v;
+  return launch(job);
+}
 
 bool gamma_ok(int g, const char *name)
 {
@@ -337,7 +461,8 @@ void do_meson(void *correl, const void *pi, const void *pj, size_t volume, int g
   set_row(p.m.ph1, kG.ph_g5g_t[gij]);
   set_row(p.m.perm2, kG.perm[gkl]);
   set_row(p.m.ph2, kG.ph_g5g_t[gkl]);
-  cuda_ok(cgb::launch_meson(job, p), "meson_two_point");
+  cuda_ok(tuned_launch(cgb::Kind::Meson, job, 0, [&](const cgb::Job &j) { return cgb::launch_meson(j, p); }),
+          "meson_two_point");
 }
 
 void do_meson_all(void **correl, const void *pi, const void *pj, size_t volume, int gamma, bool source, int prec,
@@ -393,7 +518,11 @@ void do_baryon(void *correl, const void *pi, const void *pj, const void *pn, int
   set_row(p.b.ph2[0], f.c2);
   fill_proj(p.b.proj[0], gmn, proj);
   fill_clifford(p.b.cl, proj ? &proj : nullptr, 1, gmn);
-  cuda_ok(cgb::launch_baryon(job, f.loop, p), proj ? "baryon_general_two_point" : "baryon_two_point");
+  const cgb::Kind kind = f.loop ? cgb::Kind::BaryonLoop : cgb::Kind::BaryonTri;
+  auto run = [&](const cgb::Job &j) { return cgb::launch_baryon(j, f.loop, p); };
+  // aux 0: gamma-basis triangle (one gamma), 1: triangle with N' materialised
+  const cudaError_t e = tuned_launch(kind, job, (f.loop || p.b.cl.ng == 1) ? 0 : 1, run);
+  cuda_ok(e, proj ? "baryon_general_two_point" : "baryon_two_point");
 }
 
 void do_diquark(void *dq, const void *pi, const void *pj, size_t volume, int gij, int gkl, int prec)
@@ -416,7 +545,8 @@ void do_diquark(void *dq, const void *pi, const void *pj, size_t volume, int gij
   set_row(p.b.ph1[0], kG.ph[gij]);
   set_row(p.b.perm2, kG.perm[gkl]);
   set_row(p.b.ph2[0], kG.ph_t[gkl]);
-  cuda_ok(cgb::launch_diquark(job, p), "baryon_diquark");
+  cuda_ok(tuned_launch(cgb::Kind::Diquark, job, 0, [&](const cgb::Job &j) { return cgb::launch_diquark(j, p); }),
+          "baryon_diquark");
 }
 
 void do_sequential(void *pi, void *pj, void *pn, int type, int seq, size_t volume, int gij, int gkl, int gmn, int prec)
@@ -454,7 +584,9 @@ void do_sequential(void *pi, void *pj, void *pn, int type, int seq, size_t volum
   set_row(p.b.ph1[0], f.c1);
   set_row(p.b.ph2[0], f.c2);
   fill_proj(p.b.proj[0], gmn, nullptr);
-  cuda_ok(cgb::launch_sequential(job, f.loop, role, p), "baryon_sequential_two_point");
+  cuda_ok(tuned_launch(cgb::Kind::Sequential, job, (f.loop ? 3 : 0) + role,
+                       [&](const cgb::Job &j) { return cgb::launch_sequential(j, f.loop, role, p); }),
+          "baryon_sequential_two_point");
 }
 
 } // namespace
@@ -561,6 +693,22 @@ int contract_check_device(void)
 
 void contract_set_stream(void *stream) { g_stream = static_cast<cudaStream_t>(stream); }
 
+void contract_set_autotune(int enable) { g_tune.enabled = enable ? 1 : 0; }
+
+int contract_autotune_report(char *buf, size_t n)
+{
+  std::lock_guard<std::mutex> lk(g_tune.mu);
+  std::ostringstream o;
+  for (const auto &kv : g_tune.choice) o << kv.first << '\t' << kv.second.name << '\t' << kv.second.ms << '\n';
+  const std::string r = o.str();
+  if (buf && n) {
+    const size_t m = r.size() < n - 1 ? r.size() : n - 1;
+    std::memcpy(buf, r.data(), m);
+    buf[m] = '\0';
+  }
+  return (int)g_tune.choice.size();
+}
+
 void *contract_get_stream(void) { return g_stream; }
 
 size_t contract_workspace_bytes(const int *lattice, int noutputs)
@@ -660,7 +808,9 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
   const double *pw[2] = {pr, pr + 32};
   for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
   fill_clifford(p.b.cl, pw, nproj, 0);
-  cuda_ok(cgb::launch_baryon_fused(job, nproj, p), "contract_baryon_all_types");
+  auto run = [&](const cgb::Job &j) { return cgb::launch_baryon_fused(j, nproj, p); };
+  const cudaError_t e = p.b.cl.ng <= nproj ? tuned_launch(cgb::Kind::BaryonFused, job, nproj, run) : run(job);
+  cuda_ok(e, "contract_baryon_all_types");
 }
 
 int contract_baryon_all_types_noalloc(void *correl, const void *propag_i, const void *propag_j,

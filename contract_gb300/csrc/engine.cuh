@@ -116,7 +116,20 @@ template <class Op> constexpr size_t engine_smem_bytes() { return Smem<Op>::BYTE
 // are bound by the FP64 pipe and keep one CTA with the full register file.
 template <class Op> constexpr int min_blocks()
 {
-  return (sizeof(typename Op::R) == 4 && 2 * (Smem<Op>::BYTES + 1024) <= 233472) ? 2 : 1;
+  return (sizeof(typename Op::R) == 4 && 2 * (Smem<Op>::BYTES + sizeof(typename Op::Params) + 1024) <= 233472) ? 2
+                                                                                                              : 1;
+}
+
+// The op parameters, copied to shared memory once per CTA.  Gamma tables are
+// indexed by each lane's own spin indices; from the kernel-parameter
+// (constant) space such lane-divergent loads serialise, from shared memory
+// they do not.
+template <class P> __device__ __forceinline__ void copy_params(P &dst, const P &src)
+{
+  static_assert(sizeof(P) % 4 == 0, "parameter block must be word-sized");
+  const uint32_t *s = reinterpret_cast<const uint32_t *>(&src);
+  uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
+  for (int k = threadIdx.x; k < (int)(sizeof(P) / 4); k += blockDim.x) d[k] = s[k];
 }
 
 // Running sum in the op's precision.  FP32 uses a compensated (two-sum)
@@ -213,6 +226,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) scalar_kernel(c
   constexpr int SPW = 32 / TPS, CW = Op::CW;
 
   extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(16) typename Op::Params ps;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   uint64_t *empty = full + NST;
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 120);
@@ -225,6 +239,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) scalar_kernel(c
     *abort_flag = 0;
     fence_barrier_init();
   }
+  copy_params(ps, p);
   __syncthreads();
   if (warp == 0) {
     produce<Op>(p, smem, full, empty, abort_flag);
@@ -260,7 +275,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) scalar_kernel(c
 #pragma unroll
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
     cx<R> vals[NOUT];
-    Op::site(p, in, scratch, sub, vals);
+    Op::site(ps, in, scratch, sub, vals);
 #pragma unroll
     for (int o = 0; o < NOUT; ++o) vals[o] = group_sum<TPS>(vals[o]);
     __syncwarp();
@@ -302,6 +317,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
   constexpr int SPW = 32 / TPS, CW = Op::CW;
 
   extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(16) typename Op::Params ps;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   uint64_t *empty = full + NST;
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 120);
@@ -314,6 +330,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
     *abort_flag = 0;
     fence_barrier_init();
   }
+  copy_params(ps, p);
   __syncthreads();
   if (warp == 0) {
     produce<Op>(p, smem, full, empty, abort_flag);
@@ -349,7 +366,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
 #pragma unroll
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
     unsigned char *ob = outbuf + (size_t)(u & 1) * SPW * L::SLOT;
-    Op::site(p, in, scratch, sub, reinterpret_cast<S *>(ob + (size_t)local * L::SLOT));
+    Op::site(ps, in, scratch, sub, reinterpret_cast<S *>(ob + (size_t)local * L::SLOT));
     fence_proxy_async_smem();
     __syncwarp();
     if (lane == 0) {

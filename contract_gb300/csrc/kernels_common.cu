@@ -44,6 +44,24 @@ __global__ void c64_to_c128(double2 *__restrict__ dst, const float2 *__restrict_
   }
 }
 
+int meson_variants(Prec prec, const char *const **names);
+int baryon_variants(Prec prec, int form, const char *const **names);
+int fused_variants(Prec prec, int nw, const char *const **names);
+int field_variants(Prec prec, bool sequential, const char *const **names);
+
+int launch_variants(Kind kind, Prec prec, int aux, const char *const **names)
+{
+  switch (kind) {
+  case Kind::Meson: return meson_variants(prec, names);
+  case Kind::BaryonLoop: return baryon_variants(prec, 0, names);
+  case Kind::BaryonTri: return baryon_variants(prec, aux == 0 ? 1 : 2, names);
+  case Kind::BaryonFused: return fused_variants(prec, aux, names);
+  case Kind::Diquark: return field_variants(prec, false, names);
+  case Kind::Sequential: return field_variants(prec, true, names);
+  }
+  return 1;
+}
+
 cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64)
 {
   const long long n = job.volume * 144;

@@ -1,13 +1,12 @@
 // Field-valued kernels: diquark and sequential sources.
-// Template arguments: <R, S, consumer warps, threads per site, ring stages>.
-#include "launch_impl.cuh"
+// Op template arguments: <R, S, consumer warps, threads per site, ring stages>.
+#include "launch_variants.cuh"
 
 namespace cgb {
 
-template <class R, class S, int CW, int TPS>
+template <class R, class S, int CW, int TPS, int NST>
 static cudaError_t seq_dispatch(const Job &job, bool loop, int role, const OpParams<R> &p)
 {
-  constexpr int NST = 3;
   if (loop) {
     switch (role) {
     case 0: return run_field<SequentialOp<R, S, CW, TPS, NST, true, 0>>(job, p);
@@ -22,16 +21,34 @@ static cudaError_t seq_dispatch(const Job &job, bool loop, int role, const OpPar
   }
 }
 
+// complex64 variants: the two-CTA shapes keep more tiles (and stores) in flight.
+static const VariantSet<float, 2> kDiquarkM = {
+  {run_field<DiquarkOp<float, float2, 6, 16, 2>>, run_field<DiquarkOp<float, float2, 8, 16, 3>>},
+  {"cw6.tps16.st2", "cw8.tps16.st3"},
+  0};
+
 cudaError_t launch_diquark(const Job &job, const OpParams<double> &p)
 {
   if (job.prec == Prec::C128) return run_field<DiquarkOp<double, double2, 4, 16, 3>>(job, p);
-  return run_field<DiquarkOp<float, float2, 8, 16, 3>>(job, convert_params<float>(p));
+  return kDiquarkM.launch(job, convert_params<float>(p));
 }
 
 cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParams<double> &p)
 {
-  if (job.prec == Prec::C128) return seq_dispatch<double, double2, 4, 16>(job, loop, role, p);
-  return seq_dispatch<float, float2, 8, 16>(job, loop, role, convert_params<float>(p));
+  if (job.prec == Prec::C128) return seq_dispatch<double, double2, 4, 16, 3>(job, loop, role, p);
+  const OpParams<float> q = convert_params<float>(p);
+  if (job.variant == 1) return seq_dispatch<float, float2, 8, 16, 3>(job, loop, role, q);
+  return seq_dispatch<float, float2, 5, 16, 2>(job, loop, role, q);
+}
+
+static const char *const kSequentialNames[2] = {"cw5.tps16.st2", "cw8.tps16.st3"};
+
+int field_variants(Prec prec, bool sequential, const char *const **names)
+{
+  if (prec == Prec::C128) return 1;
+  if (!sequential) return kDiquarkM.describe(names);
+  if (names) *names = kSequentialNames;
+  return 2;
 }
 
 } // namespace cgb

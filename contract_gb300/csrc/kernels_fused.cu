@@ -1,19 +1,31 @@
 // All six baryon contraction types (x up to two projectors) in one pass.
-// Template arguments: <R, S, consumer warps, threads per site, ring stages, projectors>.
-#include "launch_impl.cuh"
+// Op template arguments: <R, S, consumer warps, threads per site, ring stages, projectors>.
+#include "launch_variants.cuh"
 
 namespace cgb {
 
 // Projectors spanned by at most `nw` gamma matrices (e.g. (1 +- g4)/2): no N' buffers.
 using FusedCliff1P = BaryonFusedCliffOp<double, double2, 4, 16, 2, 1>;
 using FusedCliff2P = BaryonFusedCliffOp<double, double2, 4, 16, 2, 2>;
-using FusedCliff1M = BaryonFusedCliffOp<float, float2, 7, 16, 2, 1>;
-using FusedCliff2M = BaryonFusedCliffOp<float, float2, 7, 16, 2, 2>;
 // General projectors: N'_w = W_w N materialised per site.
 using Fused1P = BaryonFusedOp<double, double2, 4, 16, 2, 1>;
 using Fused2P = BaryonFusedOp<double, double2, 4, 16, 2, 2>;
 using Fused1M = BaryonFusedOp<float, float2, 8, 16, 2, 1>;
 using Fused2M = BaryonFusedOp<float, float2, 8, 16, 2, 2>;
+
+// complex64, FP32-issue bound: consumer warps per SM vs registers per thread.
+static const VariantSet<float, 3> kFusedCliff1M = {
+  {run_scalar<BaryonFusedCliffOp<float, float2, 7, 16, 2, 1>>,
+   run_scalar<BaryonFusedCliffOp<float, float2, 5, 16, 2, 1>>,
+   run_scalar<BaryonFusedCliffOp<float, float2, 3, 16, 3, 1>>},
+  {"cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
+  0};
+static const VariantSet<float, 3> kFusedCliff2M = {
+  {run_scalar<BaryonFusedCliffOp<float, float2, 7, 16, 2, 2>>,
+   run_scalar<BaryonFusedCliffOp<float, float2, 5, 16, 2, 2>>,
+   run_scalar<BaryonFusedCliffOp<float, float2, 3, 16, 3, 2>>},
+  {"cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
+  0};
 
 cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &p)
 {
@@ -23,8 +35,14 @@ cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &
     return nw == 1 ? run_scalar<Fused1P>(job, p) : run_scalar<Fused2P>(job, p);
   }
   const OpParams<float> q = convert_params<float>(p);
-  if (cliff) return nw == 1 ? run_scalar<FusedCliff1M>(job, q) : run_scalar<FusedCliff2M>(job, q);
+  if (cliff) return nw == 1 ? kFusedCliff1M.launch(job, q) : kFusedCliff2M.launch(job, q);
   return nw == 1 ? run_scalar<Fused1M>(job, q) : run_scalar<Fused2M>(job, q);
+}
+
+int fused_variants(Prec prec, int nw, const char *const **names)
+{
+  if (prec == Prec::C128) return 1;
+  return nw == 1 ? kFusedCliff1M.describe(names) : kFusedCliff2M.describe(names);
 }
 
 } // namespace cgb

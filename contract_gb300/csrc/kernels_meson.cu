@@ -1,22 +1,27 @@
 // Meson kernels: one Gamma pair per site, and the all-source / all-sink forms.
-// Template arguments: <R, S, consumer warps, threads per site, ring stages>.
-#include "launch_impl.cuh"
+// Op template arguments: <R, S, consumer warps, threads per site, ring stages>.
+#include "launch_variants.cuh"
 
 namespace cgb {
 
 // complex128: FP64-pipe bound; 8 sites per tile, two CTAs per SM.
 using MesonP = MesonOp<double, double2, 2, 8, 3>;
-// complex64: HBM bound; 16 sites per tile, 4-deep ring.
-using MesonM = MesonOp<float, float2, 4, 8, 4>;
 using MesonAllSrcP = MesonAllSourceOp<double, double2, 1, 3>;
 using MesonAllSnkP = MesonAllSinkOp<double, double2, 1, 3>;
 using MesonAllSrcM = MesonAllSourceOp<float, float2, 2, 4>;
 using MesonAllSnkM = MesonAllSinkOp<float, float2, 2, 4>;
 
+// complex64: HBM bound; the variants trade ring depth against CTAs per SM.
+static const VariantSet<float, 4> kMesonM = {
+  {run_scalar<MesonOp<float, float2, 4, 8, 2>>, run_scalar<MesonOp<float, float2, 4, 8, 4>>,
+   run_scalar<MesonOp<float, float2, 3, 8, 3>>, run_scalar<MesonOp<float, float2, 6, 16, 2>>},
+  {"cw4.tps8.st2", "cw4.tps8.st4", "cw3.tps8.st3", "cw6.tps16.st2"},
+  0};
+
 cudaError_t launch_meson(const Job &job, const OpParams<double> &p)
 {
   if (job.prec == Prec::C128) return run_scalar<MesonP>(job, p);
-  return run_scalar<MesonM>(job, convert_params<float>(p));
+  return kMesonM.launch(job, convert_params<float>(p));
 }
 
 cudaError_t launch_meson_all(const Job &job, bool source, const OpParams<double> &p)
@@ -25,6 +30,12 @@ cudaError_t launch_meson_all(const Job &job, bool source, const OpParams<double>
     return source ? run_scalar<MesonAllSrcP>(job, p) : run_scalar<MesonAllSnkP>(job, p);
   const OpParams<float> q = convert_params<float>(p);
   return source ? run_scalar<MesonAllSrcM>(job, q) : run_scalar<MesonAllSnkM>(job, q);
+}
+
+int meson_variants(Prec prec, const char *const **names)
+{
+  if (prec == Prec::C128) return 1;
+  return kMesonM.describe(names);
 }
 
 } // namespace cgb

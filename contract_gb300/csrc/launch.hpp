@@ -29,7 +29,18 @@ struct Job {
   int lt = 0;                // timeslices (per_site == false)
   long long half_slice = 0;  // sites per (parity, t) segment = Lx*Ly*Lz/2
   Workspace *ws = nullptr;
+  int variant = -1;          // tile-shape variant (-1: the launcher's default)
 };
+
+// Ops whose launchers offer several compiled tile shapes (consumer warps,
+// threads per site, ring stages); the autotuner in abi.cpp picks among them.
+enum class Kind { Meson = 0, BaryonLoop = 1, BaryonTri = 2, BaryonFused = 3, Diquark = 4, Sequential = 5 };
+
+// Number of variants (and their names) for an op at a precision; `aux` is
+// the projector count for BaryonFused and, for BaryonTri, 0 for the
+// gamma-basis form and 1 for the materialised-N' form.  1 means there is
+// nothing to tune.
+int launch_variants(Kind kind, Prec prec, int aux, const char *const **names);
 
 // Every launcher fills the geometry for its own tile shape and returns the
 // CUDA error of the launch (cudaSuccess when volume == 0).

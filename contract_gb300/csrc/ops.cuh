@@ -106,6 +106,24 @@ __device__ __forceinline__ void build_q(const BaryonSpin<R> &b, const S *N, S *q
   }
 }
 
+// Q_w from the gamma-basis form: Q_w = sum_k coef[w][k] sum_m i^ph[k][m] N[perm[k][m]][m].
+template <class R, class S, int TPS, int NW>
+__device__ __forceinline__ void build_q_cliff(const BaryonSpin<R> &b, const S *N, S *q, int sub)
+{
+  const CliffordSet<R> &cl = b.cl;
+  for (int e = sub; e < 9 * NW; e += TPS) {
+    const int w = e / 9, ad = e % 9;
+    cx<R> s = czero<R>();
+    for (int k = 0; k < cl.ng; ++k) {
+      cx<R> t = czero<R>();
+#pragma unroll
+      for (int m = 0; m < 4; ++m) t = cadd(t, mul_phase(ld<R>(N + (cl.perm[k][m] * 4 + m) * 9 + ad), cl.ph[k][m]));
+      cfma(s, cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t);
+    }
+    st(q + e, s);
+  }
+}
+
 // N'_w[m][l] = sum_n W[m][n] N[n][l] into the w-th scratch slot.
 template <class R, class S, int TPS, int NW>
 __device__ __forceinline__ void build_nprime(const BaryonSpin<R> &b, const S *N, S *np, int sub)
@@ -143,6 +161,25 @@ __device__ __forceinline__ void loop_site(const BaryonSpin<R> &b, const S *A, co
   using Ln = Lanes<TPS>;
   const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT;
   const int j = b.perm1[i];
+  if constexpr (Ln::LPT == 1) {
+    // One (i, l) pair per thread: contract the wedge with Q first and apply
+    // the (i, l) phases to the NV x NW scalars only.
+    cx<R> x[9], y[9], t[9];
+    load9(x, A + (i * 4 + b.perm2[l0]) * 9);
+    load9(y, B + (j * 4 + l0) * 9);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = czero<R>();
+    wedge_acc(t, x, y);
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      cx<R> qw[9];
+      load9(qw, q + w * 9);
+      const cx<R> s = dot9(t, qw);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) vals[v * NW + w] = mul_phase(s, (b.ph1[c1sel][i] + b.ph2[v][l0]) & 3u);
+    }
+    return;
+  }
   cx<R> r[NV][9];
 #pragma unroll
   for (int v = 0; v < NV; ++v)
@@ -242,8 +279,11 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
 }
 
 // Triangle form with the projectors in the gamma basis (CliffordSet):
-//   D_k = sum_m i^ph[k][m] B[perm1 i][m] ^ N[perm[k][m]][l],  s_k = A[i][perm2 l] . D_k
+//   D_k = sum_m B[perm1 i][m] ^ (i^ph[k][m] N[perm[k][m]][l]),  s_k = A[i][perm2 l] . D_k
 //   vals[v*NW + w] = c1(i) sum_l c2_v(l) sum_k coef[w][k] s_k
+// The basis term k runs outermost so that one D accumulator is live: loading
+// each B block once per term costs less than the extra registers of holding
+// every term's D (which pushed the two-CTA configuration into spills).
 template <class R, class S, int TPS, int NV, int NW>
 __device__ __forceinline__ void triangle_cliff_site(const BaryonSpin<R> &b, const S *A, const S *B, const S *N, int sub,
                                                     int c1sel, cx<R> *vals)
@@ -262,6 +302,9 @@ __device__ __forceinline__ void triangle_cliff_site(const BaryonSpin<R> &b, cons
     const int l = l0 + lo;
     cx<R> a[9];
     load9(a, A + (i * 4 + b.perm2[l]) * 9);
+    cx<R> u[NW];  // sum_k coef[w][k] s_k for this l
+#pragma unroll
+    for (int w = 0; w < NW; ++w) u[w] = czero<R>();
 #pragma unroll 1
     for (int k = 0; k < cl.ng; ++k) {
       cx<R> d[9];
@@ -273,17 +316,17 @@ __device__ __forceinline__ void triangle_cliff_site(const BaryonSpin<R> &b, cons
         cx<R> bm[9], nn[9];
         load9(bm, B + (j * 4 + m) * 9);
         load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
-        if (phased) phase9(bm, cl.ph[k][m]);
+        if (phased) phase9(nn, cl.ph[k][m]);
         wedge_acc(d, bm, nn);
       }
       const cx<R> s = dot9(a, d);
 #pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        const cx<R> t = cmul(cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(t, b.ph2[v][l]));
-      }
+      for (int w = 0; w < NW; ++w) cfma(u[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s);
     }
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(u[w], b.ph2[v][l]));
   }
   const uint32_t p1 = b.ph1[c1sel][i];
 #pragma unroll
@@ -356,7 +399,7 @@ struct BaryonFusedCliffOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
-    build_q<R, S, TPS, NW>(p.b, in[2], scratch, sub);
+    build_q_cliff<R, S, TPS, NW>(p.b, in[2], scratch, sub);
     __syncwarp();
     cx<R> t[2 * NW];
     loop_site<R, S, TPS, 2, NW>(p.b, in[0], in[1], scratch, sub, 0, t);  // IK_JL_NM, IL_JK_NM

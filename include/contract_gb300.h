@@ -67,6 +67,16 @@ int contract_check_device(void);
 void contract_set_stream(void *stream);
 void *contract_get_stream(void);
 
+/* Tile-shape autotuning (consumer warps, threads per site, ring stages) of
+ * the complex64 kernels: when enabled, the first call for a new (op, shape)
+ * times each compiled variant on its own data and keeps the fastest.  Also
+ * enabled by CONTRACT_AUTOTUNE=1; CONTRACT_TUNE_CACHE=<file> persists the
+ * choices across processes.  Never tunes during stream capture. */
+void contract_set_autotune(int enable);
+/* Writes "key<TAB>variant<TAB>ms" lines of the current choices into buf
+ * (NUL-terminated, truncated to n); returns the number of entries. */
+int contract_autotune_report(char *buf, size_t n);
+
 /* Reserve `bytes` of the per-device workspace used by per-timeslice
  * reductions, so that later calls (e.g. inside CUDA graph capture) do not
  * allocate.  Returns CONTRACT_SUCCESS or an error code. */

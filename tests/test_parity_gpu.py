@@ -158,3 +158,24 @@ def test_timeslice_deterministic(api, props):
 
 def test_device_status_clean(api):
     api.check_device()
+
+
+def test_autotuned_variants_agree(api, props, c_oracle):
+    """Every tile-shape variant the autotuner can pick computes the same result."""
+    import ctypes
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    pi, pj, pn = props
+    pp = api.projector_plus_minus()
+    ref = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp, latt=LATT).cpu().numpy()
+    lib.contract_set_autotune(1)
+    try:
+        got = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp, latt=LATT).cpu().numpy()
+        t = api.baryon(cuda(pi, True), cuda(pj, True), cuda(pn, True), 1, 5, 5, gamma_mn=8, latt=LATT).cpu().numpy()
+    finally:
+        lib.contract_set_autotune(0)
+    assert rel_err(got, ref) < 1e-6
+    site = c_oracle.baryon_two_point(pi, pj, pn, 1, 5, 5, 8)
+    assert per_t_rel(t, eo.timeslice_sum(site, LATT), site) < TOL_C64_TIMESLICE
+    buf = ctypes.create_string_buffer(4096)
+    assert lib.contract_autotune_report(buf, len(buf)) >= 2
