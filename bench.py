@@ -368,7 +368,8 @@ def run_ours(args, world, rank, local):
     return result
 
 
-PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "meson", "meson128", "meson_all",
+PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "momentum",
+               "momentum128", "meson", "meson128", "meson_all",
                "diquark", "sequential", "sequential128")
 
 
@@ -405,6 +406,12 @@ def run_profile(args):
     out = torch.empty((16, max(v, 1)), dtype=torch.complex128, device=dev)
     field = torch.empty_like(props[0])
     a, b_, c = (x.data_ptr() for x in props)
+    r = np.arange(-2, 3)
+    moms = np.ascontiguousarray(np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)[:, ::-1]
+                                .astype(np.int32))
+    moms_ptr = moms.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    mom_out = torch.empty((len(moms), latt[3], 256), dtype=torch.complex128, device=dev) if base == "momentum" \
+        else None
 
     def step():
         if base == "fused":
@@ -420,6 +427,8 @@ def run_profile(args):
             lib.contract_meson_all(ptrs, a, b_, v, 5, 1, prec, latt_c)
         elif base == "diquark":
             lib.contract_diquark(field.data_ptr(), a, b_, v, 5, 5, prec)
+        elif base == "momentum":  # all 16 x 16 meson pairs at the 125 momenta n in {-2..2}^3
+            lib.contract_meson_all_gamma_momentum(mom_out.data_ptr(), a, b_, v, latt_c, moms_ptr, len(moms), prec)
         elif base == "sequential":
             lib.contract_sequential(a, b_, c, 1, 2, v, 5, 5, 8, prec)
 

@@ -29,6 +29,7 @@ SOURCES = [
     "kernels_baryon.cu",
     "kernels_fused.cu",
     "kernels_field.cu",
+    "kernels_momentum.cu",
     "noalloc.cu",
 ]
 

@@ -24,6 +24,7 @@
 #include "contract_gb300.h"
 #include "gamma.hpp"
 #include "launch.hpp"
+#include "momentum.hpp"
 
 namespace {
 
@@ -589,6 +590,53 @@ void do_sequential(void *pi, void *pj, void *pn, int type, int seq, size_t volum
           "baryon_sequential_two_point");
 }
 
+// Build the momentum plan: distinct nx, distinct (nx, ny) pairs, FP64 phase tables.
+bool make_mom_plan(cgb::MomPlan &plan, const int *lattice, const int *moms, int nmom)
+{
+  plan = {};
+  for (int k = 0; k < 4; ++k) plan.latt[k] = lattice[k];
+  if (lattice[0] > cgb::kMomMaxL || lattice[1] > cgb::kMomMaxL || lattice[2] > cgb::kMomMaxL)
+    return invalid("momentum projection supports spatial extents up to %d", cgb::kMomMaxL);
+  if (nmom < 1 || nmom > cgb::kMomMaxP) return invalid("nmom must be 1..%d (got %d)", cgb::kMomMaxP, nmom);
+  plan.np = nmom;
+  for (int p = 0; p < nmom; ++p) {
+    const int nx = moms[3 * p], ny = moms[3 * p + 1], nz = moms[3 * p + 2];
+    int ix = -1;
+    for (int k = 0; k < plan.npx; ++k)
+      if (plan.px[k] == nx) ix = k;
+    if (ix < 0) {
+      if (plan.npx == cgb::kMomMaxPx) return invalid("at most %d distinct x momenta per call", cgb::kMomMaxPx);
+      ix = plan.npx++;
+      plan.px[ix] = nx;
+    }
+    int iq = -1;
+    for (int k = 0; k < plan.nq; ++k)
+      if (plan.q_ix[k] == ix && plan.q_ny[k] == ny) iq = k;
+    if (iq < 0) {
+      if (plan.nq == cgb::kMomMaxQ) return invalid("at most %d distinct (x, y) momentum pairs per call", cgb::kMomMaxQ);
+      iq = plan.nq++;
+      plan.q_ix[iq] = ix;
+      plan.q_ny[iq] = ny;
+    }
+    plan.p_q[p] = iq;
+    plan.p_nz[p] = nz;
+  }
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int k = 0; k < lattice[0]; ++k) {
+    plan.cosx[k] = std::cos(two_pi * k / lattice[0]);
+    plan.sinx[k] = std::sin(two_pi * k / lattice[0]);
+  }
+  for (int k = 0; k < lattice[1]; ++k) {
+    plan.cosy[k] = std::cos(two_pi * k / lattice[1]);
+    plan.siny[k] = std::sin(two_pi * k / lattice[1]);
+  }
+  for (int k = 0; k < lattice[2]; ++k) {
+    plan.cosz[k] = std::cos(two_pi * k / lattice[2]);
+    plan.sinz[k] = std::sin(two_pi * k / lattice[2]);
+  }
+  return true;
+}
+
 } // namespace
 
 // Only the C ABI is exported (the library is built with -fvisibility=hidden).
@@ -878,6 +926,29 @@ void contract_sequential(void *propag_i, void *propag_j, void *propag_n, BaryonC
 {
   do_sequential(propag_i, propag_j, propag_n, (int)contract_type, (int)sequential_type, volume, gamma_ij, gamma_kl,
                 gamma_mn, precision);
+}
+
+void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const void *propag_j, size_t volume,
+                                       const int *lattice, const int *moms, int nmom, int precision)
+{
+  if (!lattice || !moms) {
+    invalid("lattice and moms are required");
+    return;
+  }
+  if (!prec_ok(precision) || !ptr_ok(correl, volume, "correl") || !ptr_ok(propag_i, volume, "propag_i") ||
+      !ptr_ok(propag_j, volume, "propag_j"))
+    return;
+  cgb::MomPlan plan;
+  if (!make_mom_plan(plan, lattice, moms, nmom)) return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, precision, volume, lattice, &s)) return;
+  DeviceWorkspace ws(s);
+  job.ws = &ws;
+  OpParams<double> p {};
+  p.in[0] = propag_i;
+  p.in[1] = propag_j;
+  cuda_ok(cgb::launch_meson_momentum(job, p, plan, correl), "contract_meson_all_gamma_momentum");
 }
 
 } // extern "C"

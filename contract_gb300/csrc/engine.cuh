@@ -88,6 +88,13 @@ template <class S> struct SiteLayout {
   static constexpr uint32_t SLOT = SITE_BYTES + 16;
 };
 
+// Per-site output block of a field op: OUT_ELEMS complex values (a
+// propagator-shaped 144 for diquark/sequential, 256 for the all-gamma meson).
+template <class Op> struct OutLayout {
+  static constexpr uint32_t BYTES = Op::OUT_ELEMS * sizeof(typename Op::S);
+  static constexpr uint32_t SLOT = BYTES + 16;
+};
+
 // Shared-memory map of an engine kernel:
 //   [0, 128)        full[NST], empty[NST] mbarriers, abort flag
 //   stages          NST x NIN x SITES slots
@@ -102,7 +109,7 @@ template <class Op> struct Smem {
   static constexpr size_t TAIL = EXTRA + (size_t)Op::EXTRA_BYTES * Op::SITES;
   static constexpr size_t tail_bytes()
   {
-    if constexpr (Op::FIELD) return 2ull * Op::SITES * L::SLOT;
+    if constexpr (Op::FIELD) return 2ull * Op::SITES * OutLayout<Op>::SLOT;
     else return (size_t)Op::SITES * Op::NOUT * 2 * sizeof(typename Op::R);
   }
   static constexpr size_t BYTES = TAIL + tail_bytes();
@@ -342,7 +349,8 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
   const int local = lane / TPS, sub = lane % TPS;
   const int site = w * SPW + local;
   S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_BYTES);
-  unsigned char *outbuf = smem + Smem<Op>::TAIL + (size_t)w * 2 * SPW * L::SLOT;  // [2][SPW] slots
+  using O = OutLayout<Op>;
+  unsigned char *outbuf = smem + Smem<Op>::TAIL + (size_t)w * 2 * SPW * O::SLOT;  // [2][SPW] slots
 
   TileIter<SITES> it;
   it.set_chunk(g, blockIdx.x);
@@ -365,16 +373,23 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
     const S *in[NIN];
 #pragma unroll
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
-    unsigned char *ob = outbuf + (size_t)(u & 1) * SPW * L::SLOT;
-    Op::site(ps, in, scratch, sub, reinterpret_cast<S *>(ob + (size_t)local * L::SLOT));
+    unsigned char *ob = outbuf + (size_t)(u & 1) * SPW * O::SLOT;
+    Op::site(ps, in, scratch, sub, reinterpret_cast<S *>(ob + (size_t)local * O::SLOT));
     fence_proxy_async_smem();
     __syncwarp();
     if (lane == 0) {
       mbar_arrive(&empty[stage]);
-      for (int s = 0; s < SPW; ++s)
-        if (w * SPW + s < n)
-          bulk_s2g(static_cast<char *>(p.out[0]) + (first + w * SPW + s) * L::SITE_BYTES, ob + (size_t)s * L::SLOT,
-                   L::SITE_BYTES);
+      for (int s = 0; s < SPW; ++s) {
+        if (w * SPW + s >= n) continue;
+        // Destination site (identity, or a reordering such as lexicographic):
+        // checked against the volume so a bad layout cannot store out of bounds.
+        const long long dst = Op::out_index(ps, first + w * SPW + s);
+        if (dst < 0 || dst >= g.volume) {
+          report(p.status, kDevErrBadWork, (unsigned int)(first + w * SPW + s));
+          continue;
+        }
+        bulk_s2g(static_cast<char *>(p.out[0]) + dst * O::BYTES, ob + (size_t)s * O::SLOT, O::BYTES);
+      }
       bulk_commit();
       bulk_wait_read<1>();  // the other staging buffer is free again
     }

@@ -1,0 +1,131 @@
+// Meson all-gamma (16 x 16) correlators projected to momenta.
+//
+//   out[p][t][a][b] = sum_{x in t} exp(+2 pi i (nx x/Lx + ny y/Ly + nz z/Lz)) C_ab(x)
+//
+// The phase factorises over x, y and z, so instead of one dense
+// [momenta x V3] x [V3 x 256] product per timeslice (8 M N K flop) the
+// projection runs as three short transforms:
+//   1. MesonAllGammaOp (tile engine): C_ab(x) for all 256 pairs, written in
+//      lexicographic site order (HBM-bound: two propagators in, 256 complex out)
+//   2. plane_kernel: per (t, z) plane, X then Y transform of every C_ab into
+//      H[(nx, ny)][ab] (FP32 or FP64 arithmetic), stored in FP64
+//   3. momentum_finalize: Z transform and the sum over planes, in FP64.
+// For 32^3 x 64 and 125 momenta that is ~25 GFLOP instead of 537 GFLOP.
+// Phase tables exp(2 pi i k / L) are computed in FP64 on the host from the
+// exact integer index k = (n * x) mod L.
+#include "launch_variants.cuh"
+#include "momentum.hpp"
+
+namespace cgb {
+
+using MesonAllGammaP = MesonAllGammaOp<double, double2, 4, 3>;
+using MesonAllGammaM = MesonAllGammaOp<float, float2, 6, 2>;
+
+template <class R> __device__ __forceinline__ cx<R> pick(const cx<R> *g, int k)
+{
+  cx<R> r = g[0];
+#pragma unroll
+  for (int j = 1; j < kMomMaxPx; ++j)
+    if (k == j) r = g[j];
+  return r;
+}
+
+// One CTA per (z, t, chunk of (nx, ny) pairs); one thread per gamma pair.
+template <class R, class S>
+__global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, double2 *__restrict__ planes,
+                                                    const __grid_constant__ MomPlan plan)
+{
+  const int z = blockIdx.x, t = blockIdx.y, q0 = blockIdx.z * kMomQChunk, g = threadIdx.x;
+  const int lx = plan.latt[0], ly = plan.latt[1], lz = plan.latt[2];
+  const int nq = min(kMomQChunk, plan.nq - q0);
+  __shared__ R phx[kMomMaxPx][kMomMaxL][2];
+  __shared__ R phy[kMomQChunk][kMomMaxL][2];
+  for (int e = g; e < kMomMaxPx * kMomMaxL; e += blockDim.x) {
+    const int ip = e / kMomMaxL, x = e % kMomMaxL;
+    if (ip < plan.npx && x < lx) {
+      const int k = ((plan.px[ip] * x) % lx + lx) % lx;
+      phx[ip][x][0] = R(plan.cosx[k]);
+      phx[ip][x][1] = R(plan.sinx[k]);
+    }
+  }
+  for (int e = g; e < kMomQChunk * kMomMaxL; e += blockDim.x) {
+    const int q = e / kMomMaxL, y = e % kMomMaxL;
+    if (q < nq && y < ly) {
+      const int k = ((plan.q_ny[q0 + q] * y) % ly + ly) % ly;
+      phy[q][y][0] = R(plan.cosy[k]);
+      phy[q][y][1] = R(plan.siny[k]);
+    }
+  }
+  __syncthreads();
+  cx<R> h[kMomQChunk];
+#pragma unroll
+  for (int q = 0; q < kMomQChunk; ++q) h[q] = czero<R>();
+  const S *row = c + ((size_t)(t * lz + z) * ly * lx) * 256 + g;
+  for (int y = 0; y < ly; ++y) {
+    cx<R> gx[kMomMaxPx];
+#pragma unroll
+    for (int ip = 0; ip < kMomMaxPx; ++ip) gx[ip] = czero<R>();
+    for (int x = 0; x < lx; ++x) {
+      const cx<R> v = ld<R>(row + ((size_t)y * lx + x) * 256);
+#pragma unroll
+      for (int ip = 0; ip < kMomMaxPx; ++ip)
+        if (ip < plan.npx) cfma(gx[ip], cx<R> {phx[ip][x][0], phx[ip][x][1]}, v);
+    }
+#pragma unroll
+    for (int q = 0; q < kMomQChunk; ++q)
+      if (q < nq) cfma(h[q], cx<R> {phy[q][y][0], phy[q][y][1]}, pick(gx, plan.q_ix[q0 + q]));
+  }
+#pragma unroll
+  for (int q = 0; q < kMomQChunk; ++q)
+    if (q < nq)
+      planes[((size_t)(t * lz + z) * plan.nq + q0 + q) * 256 + g] = make_double2(double(h[q].x), double(h[q].y));
+}
+
+// out[p][t][g] = sum_z exp(2 pi i nz z / Lz) planes[t][z][q(p)][g], FP64.
+__global__ void __launch_bounds__(256) momentum_finalize(const double2 *__restrict__ planes, double2 *__restrict__ out,
+                                                          const __grid_constant__ MomPlan plan)
+{
+  const int ip = blockIdx.x, t = blockIdx.y, g = threadIdx.x;
+  const int lz = plan.latt[2], q = plan.p_q[ip], nz = plan.p_nz[ip];
+  double sx = 0.0, sy = 0.0;
+  for (int z = 0; z < lz; ++z) {
+    const int k = ((nz * z) % lz + lz) % lz;
+    const double c = plan.cosz[k], s = plan.sinz[k];
+    const double2 v = planes[((size_t)(t * lz + z) * plan.nq + q) * 256 + g];
+    sx += c * v.x - s * v.y;
+    sy += c * v.y + s * v.x;
+  }
+  out[((size_t)ip * plan.latt[3] + t) * 256 + g] = make_double2(sx, sy);
+}
+
+cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out)
+{
+  if (job.volume == 0) return cudaSuccess;
+  const size_t elem = job.prec == Prec::C128 ? sizeof(double2) : sizeof(float2);
+  const size_t c_bytes = ((size_t)job.volume * 256 * elem + 255) / 256 * 256;
+  const int lz = plan.latt[2], lt = plan.latt[3];
+  const size_t plane_bytes = (size_t)lt * lz * plan.nq * 256 * sizeof(double2);
+  char *ws = static_cast<char *>(job.ws->get(c_bytes + plane_bytes));
+  if (!ws) return cudaErrorMemoryAllocation;
+  double2 *planes = reinterpret_cast<double2 *>(ws + c_bytes);
+
+  OpParams<double> q = p;
+  q.out[0] = ws;
+  for (int k = 0; k < 4; ++k) q.latt[k] = plan.latt[k];
+  cudaError_t e;
+  if (job.prec == Prec::C128) e = run_field<MesonAllGammaP>(job, q);
+  else e = run_field<MesonAllGammaM>(job, convert_params<float>(q));
+  if (e != cudaSuccess) return e;
+
+  const dim3 grid(lz, lt, (plan.nq + kMomQChunk - 1) / kMomQChunk);
+  if (job.prec == Prec::C128)
+    plane_kernel<double, double2><<<grid, 256, 0, job.stream>>>(reinterpret_cast<const double2 *>(ws), planes, plan);
+  else
+    plane_kernel<float, float2><<<grid, 256, 0, job.stream>>>(reinterpret_cast<const float2 *>(ws), planes, plan);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  momentum_finalize<<<dim3(plan.np, lt), 256, 0, job.stream>>>(planes, static_cast<double2 *>(out), plan);
+  return cudaGetLastError();
+}
+
+} // namespace cgb

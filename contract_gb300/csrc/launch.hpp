@@ -65,6 +65,7 @@ template <class R> OpParams<R> convert_params(const OpParams<double> &p)
   for (int k = 0; k < 16; ++k) o.out[k] = p.out[k];
   o.geom = p.geom;
   o.status = p.status;
+  for (int k = 0; k < 4; ++k) o.latt[k] = p.latt[k];
   for (int k = 0; k < 4; ++k) {
     o.b.perm1[k] = p.b.perm1[k];
     o.b.perm2[k] = p.b.perm2[k];

@@ -74,6 +74,7 @@ template <class R> struct OpParams {
   DeviceStatus *status;
   BaryonSpin<R> b;
   MesonSpin<R> m;
+  int latt[4];  // Lx, Ly, Lz, Lt where an op needs site coordinates
 };
 
 template <int TPS> struct Lanes {
@@ -560,8 +561,9 @@ struct MesonAllSinkOp : OpBase<R, S, CW, 4, NST> {
 // with c1 from Gamma_ij, c2 from Gamma_kl^T.  Thread handles 16/TPS blocks (m, l).
 template <class R, class S, int CW, int TPS, int NST>
 struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 2, EXTRA_BYTES = 0;
+  static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 144;
   static constexpr bool FIELD = true;
+  __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)
   {
     const BaryonSpin<R> &b = p.b;
@@ -604,8 +606,9 @@ struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
 //   tri,  d/dN[perm(m)][l] = W[m][perm m] sum_i c1 c2 (A[i][perm2 l] ^ B[perm1 i][m])
 template <class R, class S, int CW, int TPS, int NST, bool LOOP, int ROLE>
 struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 2, EXTRA_BYTES = cbytes<S>(144) + 16;
+  static constexpr int NIN = 2, EXTRA_BYTES = cbytes<S>(144) + 16, OUT_ELEMS = 144;
   static constexpr bool FIELD = true;
+  __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
 
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, S *out)
   {
@@ -715,6 +718,108 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
       }
 #pragma unroll
       for (int e = 0; e < 9; ++e) st(out + dst * 9 + e, d[e]);
+    }
+  }
+};
+
+// All 16 x 16 meson gamma pairs per site, C[a][b] = meson_two_point(Gamma_a, Gamma_b)
+// (include/meson.cuh:33-50 for every pair), written as a 256-entry block per
+// site in lexicographic site order ((t*Lz + z)*Ly + y)*Lx + x for the
+// momentum projection.  Every Gamma permutes spin rows by XOR with a class
+// s = perm(0) in {0,1,2,3}.  Thread (s, i) of a site computes the 16 colour
+// dots T[k][l] = P_i[i][k] . conj(P_j[i^s][l]) -- the 256 dots of the site
+// exactly once -- then
+//   V[b] = sum_l c_b(l) T[l ^ s_b][l]                    (all 16 Gamma_b)
+//   C[a][b] += c_a(i) V[b]   for the four Gamma_a of class s,
+// summed over the four threads i by a halving shuffle exchange.
+template <class R, class S, int CW, int NST>
+struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
+  static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 256;
+  static constexpr bool FIELD = true;
+
+  __device__ static long long out_index(const OpParams<R> &p, long long site)
+  {
+    const long long lx = p.latt[0], ly = p.latt[1], lz = p.latt[2], lt = p.latt[3];
+    if (lx < 2 || ly < 1 || lz < 1 || lt < 1) return -1;  // no lattice: the engine skips and reports
+    const long long half = lx / 2;
+    long long r = site / half;
+    const long long xh = site - r * half;
+    const long long y = r % ly;
+    r /= ly;
+    const long long z = r % lz;
+    r /= lz;
+    const long long t = r % lt, par = r / lt;
+    const long long x = 2 * xh + ((par + t + z + y) & 1);
+    return ((t * lz + z) * ly + y) * lx + x;
+  }
+
+  // Gammas of each permutation class, four 4-bit indices packed per class.
+  __device__ static uint32_t class_members(int s)
+  {
+    constexpr GammaTables G = build_gamma_tables();
+    uint32_t packs[4] = {0, 0, 0, 0};
+    int fill[4] = {0, 0, 0, 0};
+    for (int n = 0; n < 16; ++n) {
+      const int c = G.perm[n][0];
+      packs[c] |= (uint32_t)n << (4 * fill[c]++);
+    }
+    return s == 0 ? packs[0] : (s == 1 ? packs[1] : (s == 2 ? packs[2] : packs[3]));
+  }
+
+  // (g5 Gamma_n)^T phase on spin row r, runtime n and r.
+  __device__ static uint32_t phase_g5g(int n, int r)
+  {
+    constexpr GammaTables G = build_gamma_tables();
+    uint32_t word[4] = {0, 0, 0, 0};  // 8 bits per gamma: four 2-bit row phases
+    for (int g = 0; g < 16; ++g)
+      for (int q = 0; q < 4; ++q) word[g >> 2] |= (uint32_t)G.ph_g5g_t[g][q] << (8 * (g & 3) + 2 * q);
+    const int wsel = n >> 2;
+    const uint32_t wv = wsel == 0 ? word[0] : (wsel == 1 ? word[1] : (wsel == 2 ? word[2] : word[3]));
+    return (wv >> (8 * (n & 3) + 2 * r)) & 3u;
+  }
+
+  __device__ static void site(const OpParams<R> &, const S *const *in, S *, int sub, S *out)
+  {
+    constexpr GammaTables G = build_gamma_tables();
+    const int s = sub >> 2, i = sub & 3, j = i ^ s;
+    cx<R> T[4][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        cx<R> t = czero<R>();
+        const S *x = in[0] + (i * 4 + k) * 9;
+        const S *y = in[1] + (j * 4 + l) * 9;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) cfma_conj(t, ld<R>(x + e), ld<R>(y + e));
+        T[k][l] = t;
+      }
+    cx<R> V[16];
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+      V[b] = czero<R>();
+#pragma unroll
+      for (int l = 0; l < 4; ++l) V[b] = cadd(V[b], mul_phase(T[G.perm[b][l]][l], G.ph_g5g_t[b][l]));
+    }
+    const uint32_t members = class_members(s);
+    const bool hi1 = i & 1, hi2 = i & 2;
+    const int b0 = (hi1 ? 8 : 0) + (hi2 ? 4 : 0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int a = (members >> (4 * q)) & 15;
+      const uint32_t pa = phase_g5g(a, i);
+      cx<R> X[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const cx<R> w_lo = mul_phase(V[k], pa), w_hi = mul_phase(V[k + 8], pa);
+        const cx<R> keep = hi1 ? w_hi : w_lo, send = hi1 ? w_lo : w_hi;
+        X[k] = cadd(keep, shfl_xor(send, 1));
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const cx<R> keep = hi2 ? X[k + 4] : X[k], send = hi2 ? X[k] : X[k + 4];
+        st(out + a * 16 + b0 + k, cadd(keep, shfl_xor(send, 2)));
+      }
     }
   }
 };

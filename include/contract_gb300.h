@@ -139,6 +139,17 @@ int contract_baryon_all_types_noalloc(void *correl, const void *propag_i, const 
                                       const void *propag_n, size_t volume, int gamma_ij, int gamma_kl, int nproj,
                                       const void *projectors, int precision, const int *lattice);
 
+/* All 16 x 16 meson correlators (C(x) of meson_two_point for every
+ * (gamma_ij, gamma_kl)) projected to momenta, per timeslice:
+ *   correl[p][t][gamma_ij * 16 + gamma_kl] =
+ *       sum_{x in t} exp(+2 pi i (nx x/Lx + ny y/Ly + nz z/Lz)) C(x),
+ * moms: HOST int[nmom][3] = (nx, ny, nz); lattice required, spatial extents
+ * <= 64, at most 8 distinct nx and 128 distinct (nx, ny) per call.  correl:
+ * device complex128 [nmom][Lt][256].  Uses the per-device workspace for
+ * V x 256 site values and the per-plane partial sums (FP64). */
+void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const void *propag_j, size_t volume,
+                                       const int *lattice, const int *moms, int nmom, int precision);
+
 /* baryon_diquark / baryon_sequential_two_point with a storage precision
  * (fields are read and written in that precision). */
 void contract_diquark(void *diquark, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
