@@ -58,6 +58,7 @@ SIGNATURES = {
                                          c_void_p, c_int, c_int_p]),
     "contract_baryon_all_types_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int,
                                                   c_int, c_void_p, c_int, c_int_p]),
+    "contract_baryon_all_types_batch": (None, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "contract_meson_all_gamma_momentum": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int_p, c_int_p, c_int,
                                                  c_int]),
     "contract_diquark": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, c_int]),

@@ -18,6 +18,7 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -25,6 +26,7 @@
 #include "gamma.hpp"
 #include "launch.hpp"
 #include "momentum.hpp"
+#include "batch.hpp"
 
 namespace {
 
@@ -949,6 +951,64 @@ void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const
   p.in[0] = propag_i;
   p.in[1] = propag_j;
   cuda_ok(cgb::launch_meson_momentum(job, p, plan, correl), "contract_meson_all_gamma_momentum");
+}
+
+void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,
+                                     int nproj, const void *projectors, int precision)
+{
+  if (nitems < 0 || nitems > 128) {
+    invalid("nitems must be 0..128 (got %d)", nitems);
+    return;
+  }
+  if (nitems == 0) return;
+  if (!items || !projectors) {
+    invalid("items and projectors are required");
+    return;
+  }
+  if (nproj < 1 || nproj > 2) {
+    invalid("nproj must be 1 or 2 (got %d)", nproj);
+    return;
+  }
+  if (!gamma_ok(gamma_ij, "gamma_ij") || !gamma_ok(gamma_kl, "gamma_kl") || !prec_ok(precision)) return;
+  std::vector<cgb::BatchSpec> specs(nitems);
+  for (int i = 0; i < nitems; ++i) {
+    const ContractBaryonBatchItem &it = items[i];
+    const int *l = it.lattice;
+    if (l[0] <= 0 || l[1] <= 0 || l[2] <= 0 || l[3] <= 0 || (l[0] & 1)) {
+      invalid("batch item %d: invalid lattice {%d, %d, %d, %d}", i, l[0], l[1], l[2], l[3]);
+      return;
+    }
+    const size_t v = (size_t)l[0] * l[1] * l[2] * l[3];
+    if (!ptr_ok(it.correl, v, "correl") || !ptr_ok(it.propag_i, v, "propag_i") ||
+        !ptr_ok(it.propag_j, v, "propag_j") || !ptr_ok(it.propag_n, v, "propag_n"))
+      return;
+    specs[i].in[0] = it.propag_i;
+    specs[i].in[1] = it.propag_j;
+    specs[i].in[2] = it.propag_n;
+    specs[i].out = static_cast<double2 *>(it.correl);
+    for (int k = 0; k < 4; ++k) specs[i].latt[k] = l[k];
+  }
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, precision, 0, nullptr, &s)) return;
+  DeviceWorkspace ws(s);
+  job.ws = &ws;
+  OpParams<double> p {};
+  set_row(p.b.perm1, kG.perm[gamma_ij]);
+  set_row(p.b.perm2, kG.perm[gamma_kl]);
+  set_row(p.b.ph1[0], kG.ph[gamma_ij]);
+  set_row(p.b.ph1[1], kG.ph_t[gamma_ij]);
+  set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);
+  set_row(p.b.ph2[1], kG.ph[gamma_kl]);
+  const double *pr = static_cast<const double *>(projectors);
+  const double *pw[2] = {pr, pr + 32};
+  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
+  fill_clifford(p.b.cl, pw, nproj, 0);
+  if (p.b.cl.ng > nproj) {
+    invalid("batched contractions need projectors spanned by at most nproj gamma matrices (got %d terms)", p.b.cl.ng);
+    return;
+  }
+  cuda_ok(cgb::launch_baryon_fused_batch(job, nproj, p, specs.data(), nitems), "contract_baryon_all_types_batch");
 }
 
 } // extern "C"

@@ -1,0 +1,257 @@
+// Persistent batched launch over a device work queue.
+//
+// A batch is up to kMaxBatch work items -- one per (source position,
+// propagator triple, lattice) -- that share one op and its spin tables.  The
+// queue travels as a kernel parameter (so it is captured by value in a CUDA
+// graph).  Each item's chunks are laid end to end in one global chunk space;
+// persistent CTAs deal global chunks round-robin exactly as the single-item
+// engine does, and for every chunk look up its item (binary search on
+// chunk_begin) for the geometry, the input pointers and the partial-sum
+// buffer.  Lattices of different extents therefore run in one launch.
+//
+// Every descriptor is validated on the device before use (extents, chunk
+// ranges, 16-byte alignment); a bad item is skipped and reported through the
+// status word as kDevErrBadWork.
+#pragma once
+
+#include "ops.cuh"
+
+namespace cgb {
+
+constexpr int kMaxBatch = 128;
+
+struct BatchItem {
+  const void *in[3];
+  double2 *partial;  // [chunks][CW][NOUT] of this item
+  TileGeom geom;     // per_site == 0: segments are half-timeslices
+  int chunk_begin;   // first global chunk of this item
+  int lt;            // timeslices (for the finalisation)
+  double2 *out;      // [NOUT][lt] complex128 result
+};
+
+template <class R> struct BatchParams {
+  OpParams<R> op;  // spin tables; op.in/op.out unused
+  DeviceStatus *status;
+  int n_items;
+  int total_chunks;
+  BatchItem items[kMaxBatch];
+};
+
+// Structural checks of one descriptor (identical in producer and consumers).
+template <int SITES, int NIN> __device__ __forceinline__ bool item_ok(const BatchItem &it)
+{
+  const TileGeom &g = it.geom;
+  if (g.seg_len <= 0 || g.num_segs <= 0 || g.chunk_tiles <= 0 || g.chunks_per_seg <= 0) return false;
+  if ((long long)g.tiles_per_seg * SITES < g.seg_len || (long long)(g.tiles_per_seg - 1) * SITES >= g.seg_len) return false;
+  if (g.total_chunks != g.chunks_per_seg * g.num_segs) return false;
+  if ((long long)g.seg_len * g.num_segs != g.volume) return false;
+  for (int q = 0; q < NIN; ++q)
+    if (!it.in[q] || (reinterpret_cast<uintptr_t>(it.in[q]) & 15)) return false;
+  return it.partial != nullptr;
+}
+
+template <class P> __device__ __forceinline__ int find_item(const P &p, int chunk)
+{
+  int lo = 0, hi = p.n_items - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (p.items[mid].chunk_begin <= chunk) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int SITES, int NIN> struct BatchIter {
+  int chunk, item, local, k, ntiles;
+  bool ok;
+
+  template <class P> __device__ __forceinline__ void set_chunk(const P &p, int c)
+  {
+    chunk = c;
+    k = 0;
+    ntiles = 0;
+    ok = false;
+    if (c >= p.total_chunks) return;
+    item = find_item(p, c);
+    const BatchItem &it = p.items[item];
+    local = c - it.chunk_begin;
+    ok = local >= 0 && local < it.geom.total_chunks && item_ok<SITES, NIN>(it);
+    if (ok) {
+      const int cc = local % it.geom.chunks_per_seg;
+      ntiles = min(it.geom.chunk_tiles, it.geom.tiles_per_seg - cc * it.geom.chunk_tiles);
+      ok = ntiles > 0;
+    }
+  }
+  template <class P> __device__ __forceinline__ bool valid(const P &p) const { return chunk < p.total_chunks; }
+  __device__ __forceinline__ bool last_in_chunk() const { return k == ntiles - 1; }
+  template <class P> __device__ __forceinline__ void next(const P &p)
+  {
+    if (!ok || ++k >= ntiles) set_chunk(p, chunk + gridDim.x);
+  }
+  template <class P> __device__ __forceinline__ void sites(const P &p, long long &first, int &n) const
+  {
+    const TileGeom &g = p.items[item].geom;
+    const int seg = local / g.chunks_per_seg;
+    const int cc = local % g.chunks_per_seg;
+    const long long t = (long long)cc * g.chunk_tiles + k;
+    first = (long long)seg * g.seg_len + t * SITES;
+    n = (int)min((long long)SITES, g.seg_len - t * SITES);
+  }
+};
+
+template <class Op>
+__device__ __forceinline__ void produce_batch(const BatchParams<typename Op::R> &p, unsigned char *smem, uint64_t *full,
+                                              uint64_t *empty, volatile int *abort_flag)
+{
+  using L = SiteLayout<typename Op::S>;
+  constexpr int NST = Op::NST, NIN = Op::NIN, SITES = Op::SITES;
+  const int lane = threadIdx.x & 31;
+  BatchIter<SITES, NIN> it;
+  it.set_chunk(p, blockIdx.x);
+  for (int u = 0; it.valid(p);) {
+    if (!it.ok) {  // a rejected descriptor: reported by the consumers, no tiles
+      it.next(p);
+      continue;
+    }
+    const int stage = u % NST;
+    if (u >= NST) {
+      const bool ok = mbar_wait_bounded(&empty[stage], ((u / NST) - 1) & 1, kWaitLimitNs);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) {
+          *abort_flag = 1;
+          report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
+        }
+        return;
+      }
+    }
+    if (*abort_flag) return;
+    long long first;
+    int n;
+    it.sites(p, first, n);
+    const BatchItem &item = p.items[it.item];
+    if (lane == 0) mbar_arrive_expect_tx(&full[stage], (uint32_t)n * NIN * L::SITE_BYTES);
+    __syncwarp();
+    unsigned char *dst = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
+    for (int c = lane; c < n * NIN; c += 32) {
+      const int q = c / n, s = c - q * n;
+      bulk_g2s(dst + ((size_t)q * SITES + s) * L::SLOT,
+               static_cast<const char *>(item.in[q]) + (first + s) * L::SITE_BYTES, L::SITE_BYTES, &full[stage]);
+    }
+    ++u;
+    it.next(p);
+  }
+}
+
+template <class Op>
+__global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_kernel(
+  const __grid_constant__ BatchParams<typename Op::R> p)
+{
+  using S = typename Op::S;
+  using R = typename Op::R;
+  using L = SiteLayout<S>;
+  constexpr int NIN = Op::NIN, SITES = Op::SITES, TPS = Op::TPS, NST = Op::NST, NOUT = Op::NOUT;
+  constexpr int SPW = 32 / TPS, CW = Op::CW;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(16) typename Op::Params ps;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);
+  uint64_t *empty = full + NST;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 120);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], CW);
+    }
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  copy_params(ps, p.op);
+  __syncthreads();
+  if (warp == 0) {
+    produce_batch<Op>(p, smem, full, empty, abort_flag);
+    return;
+  }
+
+  const int w = warp - 1;
+  const int local = lane / TPS, sub = lane % TPS;
+  const int site = w * SPW + local;
+  cx<R> *sv = reinterpret_cast<cx<R> *>(smem + Smem<Op>::TAIL) + (size_t)w * SPW * NOUT;
+  S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_BYTES);
+  ChunkSum<R> chunk_acc;
+
+  BatchIter<SITES, NIN> it;
+  it.set_chunk(p, blockIdx.x);
+  for (int u = 0; it.valid(p);) {
+    if (!it.ok) {
+      if (lane == 0 && w == 0) report(p.status, kDevErrBadWork, (unsigned int)it.chunk);
+      it.next(p);
+      continue;
+    }
+    const int stage = u % NST;
+    long long first;
+    int n;
+    it.sites(p, first, n);
+    const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, kWaitLimitNs);
+    if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
+      if (lane == 0) {
+        *abort_flag = 1;
+        report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
+        drain<NST>(full, u);
+      }
+      return;
+    }
+    const unsigned char *sb = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
+    const S *in[NIN];
+#pragma unroll
+    for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
+    cx<R> vals[NOUT];
+    Op::site(ps, in, scratch, sub, vals);
+#pragma unroll
+    for (int o = 0; o < NOUT; ++o) vals[o] = group_sum<TPS>(vals[o]);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[stage]);
+    const bool valid = site < n;
+    if (sub == 0) {
+#pragma unroll
+      for (int o = 0; o < NOUT; ++o) sv[local * NOUT + o] = valid ? vals[o] : czero<R>();
+    }
+    __syncwarp();
+    if (lane < NOUT) {
+#pragma unroll
+      for (int s = 0; s < SPW; ++s) chunk_acc.add(sv[s * NOUT + lane]);
+      if (it.last_in_chunk()) {
+        p.items[it.item].partial[((size_t)it.local * CW + w) * NOUT + lane] = chunk_acc.value();
+        chunk_acc.reset();
+      }
+    }
+    __syncwarp();
+    ++u;
+    it.next(p);
+  }
+}
+
+// out_i[o][t] = sum over parity and the item's (chunk, warp) partials, FP64,
+// fixed order.  Grid: (items, ceil(nout * max_lt / 128)).
+template <class R>
+__global__ void batch_finalize_kernel(const __grid_constant__ BatchParams<R> p, int nout, int cw)
+{
+  const int i = blockIdx.x;
+  const BatchItem &it = p.items[i];
+  const int idx = blockIdx.y * blockDim.x + threadIdx.x;
+  if (idx >= nout * it.lt || it.geom.chunks_per_seg <= 0) return;
+  const int o = idx / it.lt, t = idx % it.lt;
+  const int per_seg = it.geom.chunks_per_seg * cw;
+  double sx = 0.0, sy = 0.0;
+  for (int par = 0; par < 2; ++par) {
+    const double2 *row = it.partial + ((size_t)(par * it.lt + t) * per_seg) * nout + o;
+    for (int c = 0; c < per_seg; ++c) {
+      const double2 v = row[(size_t)c * nout];
+      sx += v.x;
+      sy += v.y;
+    }
+  }
+  it.out[(size_t)o * it.lt + t] = make_double2(sx, sy);
+}
+
+} // namespace cgb

@@ -1,0 +1,74 @@
+// Batched all-types baryon contractions: many sources / lattices per launch.
+#include "batch.cuh"
+#include "launch_impl.cuh"
+#include "batch.hpp"
+
+namespace cgb {
+
+template <class Op>
+static cudaError_t run_batch(const Job &job, const OpParams<typename Op::R> &op, const BatchSpec *specs, int n)
+{
+  using R = typename Op::R;
+  if (n <= 0) return cudaSuccess;
+  if (n > kMaxBatch) return cudaErrorInvalidValue;
+  static BatchParams<R> bp;  // large (~10 KB): built on the host, passed by value
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  bp = {};
+  bp.op = op;
+  bp.status = job.status;
+  bp.n_items = n;
+  size_t partial_total = 0;
+  int chunks = 0;
+  long long max_lt = 0;
+  for (int i = 0; i < n; ++i) {
+    Job ji = job;
+    ji.volume = (long long)specs[i].latt[0] * specs[i].latt[1] * specs[i].latt[2] * specs[i].latt[3];
+    ji.per_site = false;
+    ji.lt = specs[i].latt[3];
+    ji.half_slice = (long long)specs[i].latt[0] * specs[i].latt[1] * specs[i].latt[2] / 2;
+    BatchItem &it = bp.items[i];
+    for (int q = 0; q < 3; ++q) it.in[q] = specs[i].in[q];
+    it.geom = make_geom(ji, Op::SITES, job.num_sms);
+    it.chunk_begin = chunks;
+    it.lt = ji.lt;
+    it.out = specs[i].out;
+    chunks += it.geom.total_chunks;
+    partial_total += (size_t)it.geom.total_chunks * Op::CW * Op::NOUT;
+    max_lt = std::max<long long>(max_lt, ji.lt);
+  }
+  bp.total_chunks = chunks;
+  double2 *partial = static_cast<double2 *>(job.ws->get(partial_total * sizeof(double2)));
+  if (!partial) return cudaErrorMemoryAllocation;
+  size_t off = 0;
+  for (int i = 0; i < n; ++i) {
+    bp.items[i].partial = partial + off;
+    off += (size_t)bp.items[i].geom.total_chunks * Op::CW * Op::NOUT;
+  }
+  constexpr size_t smem = engine_smem_bytes<Op>();
+  int bps = 0;
+  cudaError_t e = prepare<Op>(batch_scalar_kernel<Op>, smem, bps);
+  if (e != cudaSuccess) return e;
+  const int grid = (int)std::min<long long>(chunks, (long long)job.num_sms * bps);
+  batch_scalar_kernel<Op><<<grid, Op::THREADS, smem, job.stream>>>(bp);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const dim3 fg(n, (unsigned)((Op::NOUT * max_lt + 127) / 128));
+  batch_finalize_kernel<R><<<fg, 128, 0, job.stream>>>(bp, Op::NOUT, Op::CW);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<double> &p, const BatchSpec *specs, int n)
+{
+  // Gamma-basis projectors only (e.g. (1 +- g4)/2): no per-site N' buffers.
+  if (p.b.cl.ng > nw) return cudaErrorInvalidValue;
+  if (job.prec == Prec::C128) {
+    return nw == 1 ? run_batch<BaryonFusedCliffOp<double, double2, 4, 16, 2, 1>>(job, p, specs, n)
+                   : run_batch<BaryonFusedCliffOp<double, double2, 4, 16, 2, 2>>(job, p, specs, n);
+  }
+  const OpParams<float> q = convert_params<float>(p);
+  return nw == 1 ? run_batch<BaryonFusedCliffOp<float, float2, 7, 16, 2, 1>>(job, q, specs, n)
+                 : run_batch<BaryonFusedCliffOp<float, float2, 7, 16, 2, 2>>(job, q, specs, n);
+}
+
+} // namespace cgb

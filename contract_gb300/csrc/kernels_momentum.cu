@@ -61,15 +61,23 @@ __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, dou
 #pragma unroll
   for (int q = 0; q < kMomQChunk; ++q) h[q] = czero<R>();
   const S *row = c + ((size_t)(t * lz + z) * ly * lx) * 256 + g;
+  constexpr int XB = 8;  // loads in flight per thread
   for (int y = 0; y < ly; ++y) {
     cx<R> gx[kMomMaxPx];
 #pragma unroll
     for (int ip = 0; ip < kMomMaxPx; ++ip) gx[ip] = czero<R>();
-    for (int x = 0; x < lx; ++x) {
-      const cx<R> v = ld<R>(row + ((size_t)y * lx + x) * 256);
+    const S *rowy = row + (size_t)y * lx * 256;
+    for (int x0 = 0; x0 < lx; x0 += XB) {
+      cx<R> v[XB];
 #pragma unroll
-      for (int ip = 0; ip < kMomMaxPx; ++ip)
-        if (ip < plan.npx) cfma(gx[ip], cx<R> {phx[ip][x][0], phx[ip][x][1]}, v);
+      for (int u = 0; u < XB; ++u) v[u] = (x0 + u < lx) ? ld<R>(rowy + (size_t)(x0 + u) * 256) : czero<R>();
+#pragma unroll
+      for (int u = 0; u < XB; ++u) {
+        if (x0 + u >= lx) break;
+#pragma unroll
+        for (int ip = 0; ip < kMomMaxPx; ++ip)
+          if (ip < plan.npx) cfma(gx[ip], cx<R> {phx[ip][x0 + u][0], phx[ip][x0 + u][1]}, v[u]);
+      }
     }
 #pragma unroll
     for (int q = 0; q < kMomQChunk; ++q)
@@ -82,20 +90,45 @@ __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, dou
 }
 
 // out[p][t][g] = sum_z exp(2 pi i nz z / Lz) planes[t][z][q(p)][g], FP64.
+// One CTA per ((nx, ny) pair q, t); each plane value is read once and feeds
+// every momentum of that pair (up to kMomMaxNzPerQ of them per pass).
+constexpr int kMomMaxNzPerQ = 16;
 __global__ void __launch_bounds__(256) momentum_finalize(const double2 *__restrict__ planes, double2 *__restrict__ out,
                                                           const __grid_constant__ MomPlan plan)
 {
-  const int ip = blockIdx.x, t = blockIdx.y, g = threadIdx.x;
-  const int lz = plan.latt[2], q = plan.p_q[ip], nz = plan.p_nz[ip];
-  double sx = 0.0, sy = 0.0;
-  for (int z = 0; z < lz; ++z) {
-    const int k = ((nz * z) % lz + lz) % lz;
-    const double c = plan.cosz[k], s = plan.sinz[k];
-    const double2 v = planes[((size_t)(t * lz + z) * plan.nq + q) * 256 + g];
-    sx += c * v.x - s * v.y;
-    sy += c * v.y + s * v.x;
+  const int q = blockIdx.x, t = blockIdx.y, g = threadIdx.x;
+  const int lz = plan.latt[2];
+  __shared__ int plist[kMomMaxP];
+  __shared__ int nlist;
+  if (g == 0) {
+    int n = 0;
+    for (int p = 0; p < plan.np; ++p)
+      if (plan.p_q[p] == q) plist[n++] = p;
+    nlist = n;
   }
-  out[((size_t)ip * plan.latt[3] + t) * 256 + g] = make_double2(sx, sy);
+  __syncthreads();
+  for (int base = 0; base < nlist; base += kMomMaxNzPerQ) {
+    const int cnt = min(kMomMaxNzPerQ, nlist - base);
+    double sx[kMomMaxNzPerQ], sy[kMomMaxNzPerQ];
+#pragma unroll
+    for (int k = 0; k < kMomMaxNzPerQ; ++k) sx[k] = sy[k] = 0.0;
+    for (int z = 0; z < lz; ++z) {
+      const double2 v = planes[((size_t)(t * lz + z) * plan.nq + q) * 256 + g];
+#pragma unroll
+      for (int k = 0; k < kMomMaxNzPerQ; ++k) {
+        if (k < cnt) {
+          const int nz = plan.p_nz[plist[base + k]];
+          const int idx = ((nz * z) % lz + lz) % lz;
+          const double c = plan.cosz[idx], s = plan.sinz[idx];
+          sx[k] += c * v.x - s * v.y;
+          sy[k] += c * v.y + s * v.x;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMomMaxNzPerQ; ++k)
+      if (k < cnt) out[((size_t)plist[base + k] * plan.latt[3] + t) * 256 + g] = make_double2(sx[k], sy[k]);
+  }
 }
 
 cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out)
@@ -124,7 +157,7 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
     plane_kernel<float, float2><<<grid, 256, 0, job.stream>>>(reinterpret_cast<const float2 *>(ws), planes, plan);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  momentum_finalize<<<dim3(plan.np, lt), 256, 0, job.stream>>>(planes, static_cast<double2 *>(out), plan);
+  momentum_finalize<<<dim3(plan.nq, lt), 256, 0, job.stream>>>(planes, static_cast<double2 *>(out), plan);
   return cudaGetLastError();
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <algorithm>
+#include <mutex>
 
 #include "launch.hpp"
 

@@ -139,6 +139,23 @@ int contract_baryon_all_types_noalloc(void *correl, const void *propag_i, const 
                                       const void *propag_n, size_t volume, int gamma_ij, int gamma_kl, int nproj,
                                       const void *projectors, int precision, const int *lattice);
 
+/* One work item of a batched launch: a source position / propagator triple
+ * on its own lattice (extents may differ between items). */
+typedef struct {
+  const void *propag_i, *propag_j, *propag_n;  /* device, `precision` storage */
+  void *correl;                                /* device complex128 [6][nproj][Lt] */
+  int lattice[4];                              /* Lx, Ly, Lz, Lt (PyQUDA even/odd order) */
+} ContractBaryonBatchItem;
+
+/* contract_baryon_all_types (per-timeslice) for up to 128 items in one
+ * persistent launch driven by a device work queue, plus one finalisation
+ * launch; items is a HOST array.  Projectors must be spanned by at most
+ * nproj gamma matrices (e.g. (1 +- g4)/2).  No host synchronisation: after a
+ * warm-up call (and contract_workspace_reserve) the sequence can be captured
+ * in a CUDA graph. */
+void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,
+                                     int nproj, const void *projectors, int precision);
+
 /* All 16 x 16 meson correlators (C(x) of meson_two_point for every
  * (gamma_ij, gamma_kl)) projected to momenta, per timeslice:
  *   correl[p][t][gamma_ij * 16 + gamma_kl] =

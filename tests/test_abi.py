@@ -166,3 +166,14 @@ def test_misaligned_pointer_rejected(lib):
         lib.contract_clear_error()
     finally:
         lib.contract_set_error_mode(0)
+
+
+def test_batch_validation_without_gpu(lib):
+    lib.contract_set_error_mode(1)
+    try:
+        lib.contract_clear_error()
+        lib.contract_baryon_all_types_batch(None, 200, 5, 5, 2, None, 1)
+        assert lib.contract_last_error() == 1 and b"nitems" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+    finally:
+        lib.contract_set_error_mode(0)
