@@ -62,6 +62,8 @@ SIGNATURES = {
     "contract_meson_all_gamma_momentum": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int_p, c_int_p, c_int,
                                                  c_int]),
     "contract_diquark": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, c_int]),
+    "contract_sequential_sink": (None, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_size_t, c_int_p, c_int, c_int,
+                                        c_int, c_int, c_int]),
     "contract_sequential": (None, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_size_t, c_int, c_int, c_int,
                                    c_int]),
 }

@@ -1011,5 +1011,45 @@ void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int n
   cuda_ok(cgb::launch_baryon_fused_batch(job, nproj, p, specs.data(), nitems), "contract_baryon_all_types_batch");
 }
 
+void contract_sequential_sink(void *propag_i, void *propag_j, void *propag_n, BaryonContractType contract_type,
+                              BaryonSequentialType sequential_type, size_t volume, const int *lattice, int t_sink,
+                              int gamma_ij, int gamma_kl, int gamma_mn, int precision)
+{
+  if (!lattice) {
+    invalid("lattice is required");
+    return;
+  }
+  if ((int)sequential_type < 0 || (int)sequential_type > 2) {
+    invalid("Invalid sequential_type value %d", (int)sequential_type);
+    return;
+  }
+  if (t_sink < 0 || t_sink >= lattice[3]) {
+    invalid("t_sink %d outside 0..%d", t_sink, lattice[3] - 1);
+    return;
+  }
+  if (!type_ok((int)contract_type) || !gamma_ok(gamma_mn, "gamma_mn") || !gamma_ok(gamma_ij, "gamma_ij") ||
+      !gamma_ok(gamma_kl, "gamma_kl") || !prec_ok(precision))
+    return;
+  if (!ptr_ok(propag_i, volume, "propag_i") || !ptr_ok(propag_j, volume, "propag_j") ||
+      !ptr_ok(propag_n, volume, "propag_n"))
+    return;
+  cgb::Job check;
+  DevState *s = nullptr;
+  if (!make_job(check, precision, volume, lattice, &s)) return;
+  const size_t site_bytes = precision == CONTRACT_C64 ? 1152 : 2304;
+  const size_t half = (size_t)check.half_slice;
+  void *bufs[3] = {propag_i, propag_j, propag_n};
+  // Zero the whole output field, then fill the sink timeslice's two
+  // (parity) segments, each a contiguous run of half-timeslice sites.
+  if (!cuda_ok(cudaMemsetAsync(bufs[(int)sequential_type], 0, volume * site_bytes, g_stream), "cudaMemsetAsync"))
+    return;
+  for (int par = 0; par < 2; ++par) {
+    const size_t off = ((size_t)par * lattice[3] + t_sink) * half * site_bytes;
+    do_sequential(static_cast<char *>(propag_i) + off, static_cast<char *>(propag_j) + off,
+                  static_cast<char *>(propag_n) + off, (int)contract_type, (int)sequential_type, half, gamma_ij,
+                  gamma_kl, gamma_mn, precision);
+  }
+}
+
 } // extern "C"
 #pragma GCC visibility pop

@@ -175,6 +175,14 @@ void contract_sequential(void *propag_i, void *propag_j, void *propag_n, BaryonC
                          BaryonSequentialType sequential_type, size_t volume, int gamma_ij, int gamma_kl,
                          int gamma_mn, int precision);
 
+/* Sequential source inserted at the sink timeslice t_sink: the selected
+ * propagator is overwritten with dC(x)/dP(x) on the sites of timeslice
+ * t_sink and with zeros everywhere else (PyQUDA even/odd order, lattice
+ * required). */
+void contract_sequential_sink(void *propag_i, void *propag_j, void *propag_n, BaryonContractType contract_type,
+                              BaryonSequentialType sequential_type, size_t volume, const int *lattice, int t_sink,
+                              int gamma_ij, int gamma_kl, int gamma_mn, int precision);
+
 #ifdef __cplusplus
 }
 #endif

@@ -278,3 +278,25 @@ def test_batched_work_queue_and_cuda_graph(api, c64):
     for out, ref in zip(outs, refs):
         assert rel_err(out.cpu().numpy(), ref) < 1e-12
     api.check_device()
+
+
+@pytest.mark.parametrize("c64", [False, True])
+def test_sequential_sink_timeslice(api, props, c_oracle, c64):
+    """Sequential source at t_sink: dC/dP on that timeslice, zero elsewhere."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    pi, pj, pn = props
+    v = pi.shape[0]
+    _, _, _, tt = eo.eo_coords(LATT)
+    lat = (ctypes.c_int * 4)(*LATT)
+    for ct, slot, t_sink in ((1, 2, 3), (0, 0, 7), (4, 1, 0)):
+        ref = c_oracle.baryon_sequential(pi, pj, pn, ct, slot, 5, 5, 8)
+        ref[tt != t_sink] = 0
+        bufs = [cuda(p, c64) for p in (pi, pj, pn)]
+        lib.contract_sequential_sink(*[b.data_ptr() for b in bufs], ct, slot, v, lat, t_sink, 5, 5, 8, 1 if c64 else 0)
+        got = bufs[slot].to(torch.complex128).cpu().numpy()
+        assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+        assert np.count_nonzero(got[tt != t_sink]) == 0
+        assert rel_err(got, ref) < (1e-6 if c64 else TOL_C128), (ct, slot, t_sink)
