@@ -87,7 +87,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
@@ -150,6 +150,12 @@ def max_over_ranks(x, world, device=None):
     t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(units_per_rank, ms_max, world):
+    """Whole-job GSite/s of `world` independent replicas: every rank processes
+    `units_per_rank` site-contractions and the job takes the slowest rank's time."""
+    return world * units_per_rank / (ms_max * 1e-3) / 1e9
 
 
 # ------------------------------------------------------------ CPU baseline --
@@ -267,7 +273,7 @@ def run_ours(args, world, rank, local):
     with ClockSampler(local) as clocks:
         ms_mixed = timed(lambda: fused(out64, u64, u264, d64, 1), args.steps, args.warmup)
     ms_mixed = max_over_ranks(ms_mixed, world, dev)
-    value = world * units / (ms_mixed * 1e-3) / 1e9
+    value = replica_value(units, ms_mixed, world)
 
     # ---- plain complex128 forms: fused, and the drop-in per-call sequence
     plain_steps = max(1, min(args.steps, 5))
@@ -346,7 +352,7 @@ def run_ours(args, world, rank, local):
             "hbm_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "scalar_kernel<BaryonFusedOp<float,float2,...,NW=2>> + finalize",
+                         "kernel": "scalar_kernel<BaryonFusedCliffOp<float,float2,...,NW=2>> + finalize_kernel",
                          "algorithmic_bytes_per_launch": bytes_per_launch},
             "fp32_pipe": {"achieved_tflops": flops_per_launch / (ms_mixed * 1e-3) / 1e12,
                           "peak_tflops": 73.1, "peak_source": "measured FFMA probe",
@@ -366,6 +372,209 @@ def run_ours(args, world, rank, local):
         }
         print(json.dumps(result), flush=True)
     return result
+
+
+# ------------------------------------------------------- other workloads --
+# Further BASELINE configurations, measured on request (the default run is
+# the 24^3 x 64 baryon workload above).
+
+def _gpu_env():
+    import torch
+
+    from contract_gb300 import _lib, api, build
+    build.build()
+    lib = _lib.lib()
+    lib.contract_set_error_mode(1)
+    lib.contract_set_autotune(1)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    lib.contract_set_stream(stream.cuda_stream)
+    return torch, lib, api, dev, stream
+
+
+def _time(torch, stream, fn, steps, warmup, lib):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    if lib.contract_last_error():
+        raise RuntimeError(lib.contract_last_error_message().decode())
+    return e0.elapsed_time(e1) / steps
+
+
+def _rel(a, b):
+    r = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+    return {"max_rel_err": float(r.max()), "median_rel_err": float(np.median(r)),
+            "frac_le_1e-6": float((r <= 1e-6).mean()),
+            "max_err_rel_to_max": float(np.abs(a - b).max() / np.abs(b).max())}
+
+
+def workload_momentum32(args):
+    """BASELINE config 3: all 16 x 16 meson pairs at 125 momenta on 32^3 x 64."""
+    torch, lib, api, dev, stream = _gpu_env()
+    from contract_gb300.lattice import synthetic_propagator
+    latt = (32, 32, 32, 64)
+    v = latt[0] * latt[1] * latt[2] * latt[3]
+    p1 = synthetic_propagator(latt, 11, 0.2, device=dev)
+    p2 = synthetic_propagator(latt, 12, 0.2, device=dev)
+    q1, q2 = api.to_c64(p1), api.to_c64(p2)
+    r = np.arange(-2, 3)
+    moms = np.ascontiguousarray(np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)[:, ::-1]
+                                .astype(np.int32))
+    mp = moms.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    lat = (ctypes.c_int * 4)(*latt)
+    out64 = torch.empty((len(moms), latt[3], 256), dtype=torch.complex128, device=dev)
+    out128 = torch.empty_like(out64)
+    ms64 = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
+        out64.data_ptr(), q1.data_ptr(), q2.data_ptr(), v, lat, mp, len(moms), 1), args.steps, args.warmup, lib)
+    ms128 = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
+        out128.data_ptr(), p1.data_ptr(), p2.data_ptr(), v, lat, mp, len(moms), 0), 2, 1, lib)
+    units = v * 256
+    dense_flop = 8.0 * len(moms) * 256 * v  # the per-timeslice dense GEMM this replaces
+    print(json.dumps({"workload": "momentum32", "lattice": list(latt), "momenta": len(moms), "pairs": 256,
+                      "mixed_ms": ms64, "plain_ms": ms128, "mixed_gsite_s": units / ms64 / 1e6,
+                      "plain_gsite_s": units / ms128 / 1e6, "speedup": ms128 / ms64,
+                      "dense_gemm_equiv_tflops_mixed": dense_flop / ms64 / 1e9,
+                      "accuracy_mixed_vs_plain": _rel(out64.cpu().numpy(), out128.cpu().numpy())}), flush=True)
+
+
+def workload_sequential48(args):
+    """BASELINE config 4 on 48^3 x 96: the sequential source (full volume, and
+    the t_sink = 24 insertion with zeros elsewhere), then a zero-momentum
+    baryon_general two-point with (1 + g4)/2; complex128 vs complex64 storage
+    of the same propagator values."""
+    torch, lib, api, dev, stream = _gpu_env()
+    from contract_gb300.lattice import synthetic_propagator
+    latt = (48, 48, 48, 96)
+    v = latt[0] * latt[1] * latt[2] * latt[3]
+    lat = (ctypes.c_int * 4)(*latt)
+    pp = np.ascontiguousarray(api.projector_plus_minus())
+    res = {"workload": "sequential48", "lattice": list(latt), "t_sink": 24, "type": "IK_JL_NM",
+           "sequential": "SEQUENTIAL_N (writes propag_n)", "gamma": "C g5, C g5, g4"}
+    u128 = synthetic_propagator(latt, 21, 0.25, device=dev)
+    d128 = synthetic_propagator(latt, 23, 0.30, device=dev)
+    seq128 = torch.empty_like(u128)
+    kept = {}
+    for name, prec in (("c128", 0), ("c64", 1)):
+        u, d = (u128, d128) if prec == 0 else (api.to_c64(u128), api.to_c64(d128))
+        seq = seq128 if prec == 0 else torch.empty_like(u)
+        corr = torch.empty(latt[3], dtype=torch.complex128, device=dev)
+        site = 1152 if prec else 2304
+        ms_full = _time(torch, stream, lambda: lib.contract_sequential(
+            u.data_ptr(), u.data_ptr(), seq.data_ptr(), 0, 2, v, 5, 5, 8, prec), args.steps, args.warmup, lib)
+        ms_sink = _time(torch, stream, lambda: lib.contract_sequential_sink(
+            u.data_ptr(), u.data_ptr(), seq.data_ptr(), 0, 2, v, lat, 24, 5, 5, 8, prec), args.steps, args.warmup, lib)
+        ms_2pt = _time(torch, stream, lambda: lib.contract_baryon(
+            corr.data_ptr(), u.data_ptr(), u.data_ptr(), d.data_ptr(), 0, v, 5, 5, 0, pp[0].ctypes.data, prec, lat),
+            args.steps, args.warmup, lib)
+        slab = seq.view(2, latt[3], -1)[:, 24].to(torch.complex128)
+        kept[name] = (corr.cpu().numpy(), slab)
+        res[name] = {"sequential_full_ms": ms_full, "sequential_full_gbs": 3 * v * site / ms_full / 1e6,
+                     "sequential_full_gsite_s": v / ms_full / 1e6,
+                     "sequential_sink_ms": ms_sink, "sequential_sink_write_gbs": v * site / ms_sink / 1e6,
+                     "twopt_ms": ms_2pt, "twopt_gbs": 3 * v * site / ms_2pt / 1e6, "twopt_gsite_s": v / ms_2pt / 1e6}
+        if prec:
+            del u, d, seq
+            torch.cuda.empty_cache()
+    c128, s128 = kept["c128"]
+    c64, s64 = kept["c64"]
+    res["speedup_c64_vs_c128"] = {k: res["c128"][k] / res["c64"][k] for k in
+                                  ("sequential_full_ms", "sequential_sink_ms", "twopt_ms")}
+    res["accuracy_c64_vs_c128"] = {
+        "twopt": _rel(c64, c128),
+        "sink_slab_max_err_rel_to_max": float((s64 - s128).abs().max() / s128.abs().max())}
+    print(json.dumps(res), flush=True)
+
+
+def workload_batch(args):
+    """BASELINE config 5: 64 sources on 16^3x32, 24^3x48 and 32^3x64 lattices,
+    each with the 16 x 16 meson at 27 momenta and all baryon types, as one
+    CUDA graph (batched baryon launch + per-source meson pipeline), complex64;
+    compared with the plain per-call FP64 form on one source per lattice."""
+    torch, lib, api, dev, stream = _gpu_env()
+    from contract_gb300.lattice import synthetic_propagator
+    classes = [((16, 16, 16, 32), 24), ((24, 24, 24, 48), 24), ((32, 32, 32, 64), 16)]
+    rng = np.random.default_rng(5)
+    r = np.arange(-1, 2)
+    moms = np.ascontiguousarray(np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)[:, ::-1]
+                                .astype(np.int32))
+    mp = moms.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    pp = np.ascontiguousarray(api.projector_plus_minus())
+
+    class Item(ctypes.Structure):
+        _fields_ = [("propag_i", ctypes.c_void_p), ("propag_j", ctypes.c_void_p), ("propag_n", ctypes.c_void_p),
+                    ("correl", ctypes.c_void_p), ("lattice", ctypes.c_int * 4)]
+
+    sources = []
+    seed = 1000
+    for latt, count in classes:
+        for _ in range(count):
+            mu, md = rng.uniform(0.1, 0.5, 2)
+            u = synthetic_propagator(latt, seed, float(mu), device=dev, dtype=torch.complex64)
+            d = synthetic_propagator(latt, seed + 1, float(md), device=dev, dtype=torch.complex64)
+            seed += 2
+            sources.append({"latt": latt, "u": u, "d": d, "mu": float(mu), "md": float(md),
+                            "bary": torch.empty((6, 2, latt[3]), dtype=torch.complex128, device=dev),
+                            "mes": torch.empty((len(moms), latt[3], 256), dtype=torch.complex128, device=dev)})
+    items = (Item * len(sources))()
+    for k, s in enumerate(sources):
+        items[k].propag_i = items[k].propag_j = s["u"].data_ptr()
+        items[k].propag_n = s["d"].data_ptr()
+        items[k].correl = s["bary"].data_ptr()
+        items[k].lattice = (ctypes.c_int * 4)(*s["latt"])
+    lats = [(ctypes.c_int * 4)(*s["latt"]) for s in sources]
+
+    def step():
+        lib.contract_baryon_all_types_batch(items, len(sources), 5, 5, 2, pp.ctypes.data, 1)
+        for s, lat in zip(sources, lats):
+            vs = s["u"].numel() // 144
+            lib.contract_meson_all_gamma_momentum(s["mes"].data_ptr(), s["u"].data_ptr(), s["u"].data_ptr(), vs, lat,
+                                                  mp, len(moms), 1)
+
+    step()  # autotune + workspace growth before capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        lib.contract_set_stream(torch.cuda.current_stream().cuda_stream)
+        step()
+    lib.contract_set_stream(stream.cuda_stream)
+    ms_graph = _time(torch, stream, g.replay, args.steps, args.warmup, lib)
+    sites = sum(s["u"].numel() // 144 for s in sources)
+    # plain per-call FP64 on the first source of each lattice class, extrapolated by site count
+    plain_ms_total, errs = 0.0, []
+    first = 0
+    for latt, count in classes:
+        s = sources[first]
+        first += count
+        u, d = s["u"].to(torch.complex128), s["d"].to(torch.complex128)
+        vs = u.numel() // 144
+        lat = (ctypes.c_int * 4)(*latt)
+        bary = torch.empty((6, 2, latt[3]), dtype=torch.complex128, device=dev)
+        mes = torch.empty_like(s["mes"])
+
+        def plain():
+            for t in range(6):
+                for w in range(2):
+                    lib.contract_baryon(bary[t, w].data_ptr(), u.data_ptr(), u.data_ptr(), d.data_ptr(), t, vs, 5, 5, 0,
+                                        pp[w].ctypes.data, 0, lat)
+            lib.contract_meson_all_gamma_momentum(mes.data_ptr(), u.data_ptr(), u.data_ptr(), vs, lat, mp, len(moms), 0)
+
+        plain_ms_total += _time(torch, stream, plain, 1, 1, lib) * count
+        errs.append({"lattice": list(latt), "baryon": _rel(s["bary"].cpu().numpy(), bary.cpu().numpy()),
+                     "meson": _rel(s["mes"].cpu().numpy(), mes.cpu().numpy())})
+    print(json.dumps({"workload": "batch", "sources": len(sources), "site_sources": sites,
+                      "contractions_per_site": {"baryon": 12, "meson_pairs": 256, "momenta": len(moms)},
+                      "mixed_graph_ms": ms_graph, "plain_per_call_ms_extrapolated": plain_ms_total,
+                      "speedup": plain_ms_total / ms_graph,
+                      "baryon_gsite_s": sites * 12 / ms_graph / 1e6, "accuracy_mixed_vs_plain": errs}), flush=True)
+
+
+WORKLOADS = {"momentum32": workload_momentum32, "sequential48": workload_sequential48, "batch": workload_batch}
 
 
 PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "momentum",
@@ -450,7 +659,7 @@ def run_profile(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--cpu-slices", type=int, default=8, help="timeslices in the CPU baseline sample")
@@ -458,9 +667,13 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="use the default tile shapes")
     ap.add_argument("--profile", choices=PROFILE_OPS, help="run only this op (for ncu captures)")
     ap.add_argument("--lattice", default="24,24,24,16", help="Lx,Ly,Lz,Lt for --profile")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), help="measure another BASELINE configuration")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
+        return
+    if args.workload:
+        WORKLOADS[args.workload](args)
         return
     world, rank, local = dist_setup(args)
     try:
