@@ -432,15 +432,22 @@ def workload_momentum32(args):
     out128 = torch.empty_like(out64)
     ms64 = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
         out64.data_ptr(), q1.data_ptr(), q2.data_ptr(), v, lat, mp, len(moms), 1), args.steps, args.warmup, lib)
+    outtc = torch.empty_like(out64)
+    ms_tc = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
+        outtc.data_ptr(), q1.data_ptr(), q2.data_ptr(), v, lat, mp, len(moms), 2), args.steps, args.warmup, lib)
     ms128 = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
         out128.data_ptr(), p1.data_ptr(), p2.data_ptr(), v, lat, mp, len(moms), 0), 2, 1, lib)
     units = v * 256
-    dense_flop = 8.0 * len(moms) * 256 * v  # the per-timeslice dense GEMM this replaces
+    dense_flop = 8.0 * len(moms) * 256 * v  # the per-timeslice dense complex GEMM
+    ref = out128.cpu().numpy()
     print(json.dumps({"workload": "momentum32", "lattice": list(latt), "momenta": len(moms), "pairs": 256,
-                      "mixed_ms": ms64, "plain_ms": ms128, "mixed_gsite_s": units / ms64 / 1e6,
-                      "plain_gsite_s": units / ms128 / 1e6, "speedup": ms128 / ms64,
+                      "mixed_ms": ms64, "tensor_ms": ms_tc, "plain_ms": ms128, "mixed_gsite_s": units / ms64 / 1e6,
+                      "tensor_gsite_s": units / ms_tc / 1e6, "plain_gsite_s": units / ms128 / 1e6,
+                      "speedup": ms128 / ms64, "speedup_tensor": ms128 / ms_tc,
                       "dense_gemm_equiv_tflops_mixed": dense_flop / ms64 / 1e9,
-                      "accuracy_mixed_vs_plain": _rel(out64.cpu().numpy(), out128.cpu().numpy())}), flush=True)
+                      "dense_gemm_equiv_tflops_tensor": dense_flop / ms_tc / 1e9,
+                      "accuracy_mixed_vs_plain": _rel(out64.cpu().numpy(), ref),
+                      "accuracy_tensor_vs_plain": _rel(outtc.cpu().numpy(), ref)}), flush=True)
 
 
 def workload_sequential48(args):
@@ -578,7 +585,7 @@ WORKLOADS = {"momentum32": workload_momentum32, "sequential48": workload_sequent
 
 
 PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "momentum",
-               "momentum128", "meson", "meson128", "meson_all",
+               "momentum128", "momentum_tc", "meson", "meson128", "meson_all",
                "diquark", "sequential", "sequential128")
 
 
@@ -619,8 +626,8 @@ def run_profile(args):
     moms = np.ascontiguousarray(np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)[:, ::-1]
                                 .astype(np.int32))
     moms_ptr = moms.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
-    mom_out = torch.empty((len(moms), latt[3], 256), dtype=torch.complex128, device=dev) if base == "momentum" \
-        else None
+    mom_out = torch.empty((len(moms), latt[3], 256), dtype=torch.complex128, device=dev) \
+        if base.startswith("momentum") else None
 
     def step():
         if base == "fused":
@@ -638,6 +645,8 @@ def run_profile(args):
             lib.contract_diquark(field.data_ptr(), a, b_, v, 5, 5, prec)
         elif base == "momentum":  # all 16 x 16 meson pairs at the 125 momenta n in {-2..2}^3
             lib.contract_meson_all_gamma_momentum(mom_out.data_ptr(), a, b_, v, latt_c, moms_ptr, len(moms), prec)
+        elif base == "momentum_tc":  # the same on the tensor cores (split bf16)
+            lib.contract_meson_all_gamma_momentum(mom_out.data_ptr(), a, b_, v, latt_c, moms_ptr, len(moms), 2)
         elif base == "sequential":
             lib.contract_sequential(a, b_, c, 1, 2, v, 5, 5, 8, prec)
 

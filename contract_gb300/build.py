@@ -30,6 +30,7 @@ SOURCES = [
     "kernels_fused.cu",
     "kernels_field.cu",
     "kernels_momentum.cu",
+    "kernels_momentum_tc.cu",
     "kernels_batch.cu",
     "noalloc.cu",
 ]

@@ -937,6 +937,8 @@ void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const
     invalid("lattice and moms are required");
     return;
   }
+  const bool tensor_cores = precision == CONTRACT_C64_TC;
+  if (tensor_cores) precision = CONTRACT_C64;
   if (!prec_ok(precision) || !ptr_ok(correl, volume, "correl") || !ptr_ok(propag_i, volume, "propag_i") ||
       !ptr_ok(propag_j, volume, "propag_j"))
     return;
@@ -950,7 +952,7 @@ void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const
   OpParams<double> p {};
   p.in[0] = propag_i;
   p.in[1] = propag_j;
-  cuda_ok(cgb::launch_meson_momentum(job, p, plan, correl), "contract_meson_all_gamma_momentum");
+  cuda_ok(cgb::launch_meson_momentum(job, p, plan, correl, tensor_cores), "contract_meson_all_gamma_momentum");
 }
 
 void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,

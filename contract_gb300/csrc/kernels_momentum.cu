@@ -131,13 +131,18 @@ __global__ void __launch_bounds__(256) momentum_finalize(const double2 *__restri
   }
 }
 
-cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out)
+cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out,
+                                  bool tensor_cores)
 {
   if (job.volume == 0) return cudaSuccess;
+  if (tensor_cores && job.prec != Prec::C64) return cudaErrorInvalidValue;
   const size_t elem = job.prec == Prec::C128 ? sizeof(double2) : sizeof(float2);
   const size_t c_bytes = ((size_t)job.volume * 256 * elem + 255) / 256 * 256;
   const int lz = plan.latt[2], lt = plan.latt[3];
-  const size_t plane_bytes = (size_t)lt * lz * plan.nq * 256 * sizeof(double2);
+  const TcGeom tg = make_tc_geom(plan);
+  const size_t a_bytes = (tc_phase_bytes(tg) + 255) / 256 * 256;
+  const size_t plane_bytes = tensor_cores ? a_bytes + tc_partial_bytes(tg)
+                                          : (size_t)lt * lz * plan.nq * 256 * sizeof(double2);
   char *ws = static_cast<char *>(job.ws->get(c_bytes + plane_bytes));
   if (!ws) return cudaErrorMemoryAllocation;
   double2 *planes = reinterpret_cast<double2 *>(ws + c_bytes);
@@ -149,6 +154,9 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   if (job.prec == Prec::C128) e = run_field<MesonAllGammaP>(job, q);
   else e = run_field<MesonAllGammaM>(job, convert_params<float>(q));
   if (e != cudaSuccess) return e;
+  if (tensor_cores)
+    return launch_momentum_tc(job, plan, tg, ws, reinterpret_cast<unsigned char *>(ws + c_bytes),
+                              reinterpret_cast<float *>(ws + c_bytes + a_bytes), out);
 
   const dim3 grid(lz, lt, (plan.nq + kMomQChunk - 1) / kMomQChunk);
   if (job.prec == Prec::C128)

@@ -1,0 +1,429 @@
+// Momentum projection on the tensor cores (tcgen05), complex64 storage.
+//
+// Per timeslice t the projection is the complex GEMM
+//   D[p][n] = sum_s Phi[p][s] C[s][n],   Phi[p][s] = exp(+2 pi i (nx x / Lx + ny y / Ly + nz z / Lz)),
+// s the lexicographic site of the timeslice and n the 256 (Gamma_ij, Gamma_kl)
+// pairs.  It runs as one real GEMM with the momentum rows doubled and the
+// site columns interleaved (re, im):
+//   A'[2p  ][2s] =  Re Phi   A'[2p  ][2s+1] = -Im Phi   ->  D'[2p  ][n] = Re D[p][n]
+//   A'[2p+1][2s] =  Im Phi   A'[2p+1][2s+1] =  Re Phi   ->  D'[2p+1][n] = Im D[p][n]
+//   B'[n][2s + c] = (Re C[s][n], Im C[s][n])[c]
+// Every operand value x is split into two bf16 terms, hi = bf16(x) and
+// lo = bf16(x - hi), and the product keeps hi*hi + hi*lo + lo*hi ("split
+// bf16, three products"); the tensor core accumulates in FP32 in tensor
+// memory.  A k-step is 8 sites (K = 16 of the real GEMM).
+//
+// Work: units (momentum group of 128, block of k-steps, t, pair half) are
+// dealt round-robin to persistent CTAs, so the CTAs running together share
+// the same phase tiles (L2-resident; the phase matrix does not depend on t).
+// Roles in a CTA (320 threads):
+//   warp 0     TMA producer: per k-step one 16 KB phase tile (both m-tiles,
+//              hi and lo, pre-tiled in global memory) and up to eight 1 KB
+//              rows of the complex64 per-site field into a staging buffer
+//   warp 1     allocates the 512 TMEM columns and issues the MMAs: for each
+//              of the two 128-row m-tiles three M=128, N=128, K=16 MMAs per
+//              k-step, into one of two accumulator buffers
+//   warps 2-9  convert the staged FP32 values into the bf16 hi/lo operand
+//              tiles, and every kTcFlush k-steps move an accumulator buffer
+//              into FP32 registers (tcgen05.ld) and release it; at the end
+//              of a unit they store its 256 x 128 FP32 partial
+// A final kernel sums the partials of each (t, p, n) in FP64 in a fixed order.
+// Every mbarrier wait is bounded; on a timeout the CTA stops, reports
+// kDevErrWaitTimeout, waits (bounded) for its copies and MMAs and frees TMEM.
+#include <cuda_bf16.h>
+
+#include "engine.cuh"
+#include "momentum.hpp"
+#include "tc.cuh"
+
+namespace cgb {
+
+namespace {
+
+constexpr int kTcStages = 6;
+constexpr int kTcFlush = 4;       // k-steps per accumulator buffer
+constexpr int kTcThreads = 320;
+constexpr int kTcHeader = 1024;   // barriers, TMEM slot, abort flag
+constexpr int kTcABytes = 16384;  // 2 m-tiles x {hi, lo} x 128 x 16 bf16
+constexpr int kTcBBytes = 8192;   // {hi, lo} x 128 x 16 bf16
+constexpr int kTcStgBytes = 8192; // 8 sites x 128 pairs x complex64
+constexpr int kTcStageBytes = kTcABytes + kTcBBytes + kTcStgBytes;
+constexpr int kTcSmem = kTcHeader + kTcStages * kTcStageBytes;
+constexpr uint32_t kTcIdesc = umma_idesc_bf16(128, 128);
+constexpr uint32_t kTcLbo = 16 * 128, kTcSbo = 128;  // 128-row tiles
+
+struct TcParams {
+  const float2 *field;          // [Lt][V3][256] complex64, lexicographic sites
+  const unsigned char *atiles;  // [MG][J][m-tile][hi, lo][4096 B]
+  float *partial;               // [U][m-tile][128 rows][128 pairs]
+  DeviceStatus *status;
+  TcGeom g;
+};
+
+struct Unit {
+  int mg, jb, t, h, j0, j1;
+};
+
+__device__ __forceinline__ Unit decode(const TcGeom &g, int u)
+{
+  Unit w;
+  w.h = u & 1;
+  int r = u >> 1;
+  w.t = r % g.lt;
+  r /= g.lt;
+  w.jb = r % g.jb;
+  w.mg = r / g.jb;
+  w.j0 = w.jb * g.ku;
+  w.j1 = min(g.j, w.j0 + g.ku);
+  return w;
+}
+
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
+
+// (a, b) -> packed bf16 hi and lo terms (a in the low half).
+__device__ __forceinline__ void split2(float a, float b, uint32_t &hi, uint32_t &lo)
+{
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  hi = bf16x2_bits(h);
+  lo = bf16x2_bits(__floats2bfloat162_rn(a - hf.x, b - hf.y));
+}
+
+__device__ __forceinline__ void tc_abort(volatile int *abort_flag, DeviceStatus *st, unsigned int where)
+{
+  *abort_flag = 1;
+  report(st, kDevErrWaitTimeout, where);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_constant__ TcParams p)
+{
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t *ld_full = reinterpret_cast<uint64_t *>(smem);
+  uint64_t *op_full = ld_full + kTcStages;
+  uint64_t *op_empty = op_full + kTcStages;
+  uint64_t *acc_full = op_empty + kTcStages;
+  uint64_t *acc_empty = acc_full + 2;
+  uint64_t *fin = acc_empty + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 512);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 516);
+  unsigned char *stages = smem + kTcHeader;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const TcGeom &g = p.g;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTcStages; ++s) {
+      mbar_init(&ld_full[s], 1);
+      mbar_init(&op_full[s], 8);
+      mbar_init(&op_empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 8);
+    }
+    mbar_init(fin, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_slot, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------- TMA producer
+    uint32_t gi = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
+      const Unit w = decode(g, u);
+      for (int j = w.j0; j < w.j1; ++j, ++gi) {
+        const int s = gi % kTcStages;
+        if (gi >= kTcStages) {
+          ok = __all_sync(0xffffffffu, mbar_wait_bounded(&op_empty[s], ((gi / kTcStages) - 1) & 1, kWaitLimitNs));
+          if (!ok) {
+            if (lane == 0) tc_abort(abort_flag, p.status, 0x100000u | (unsigned)u);
+            break;
+          }
+        }
+        if (*abort_flag) {
+          ok = false;
+          break;
+        }
+        const long long s0 = (long long)j * 8;
+        const int nvalid = (int)min(8LL, g.v3 - s0);
+        unsigned char *st = stages + s * kTcStageBytes;
+        if (lane == 0) mbar_arrive_expect_tx(&ld_full[s], (uint32_t)(kTcABytes + nvalid * 1024));
+        __syncwarp();
+        if (lane == 0)
+          bulk_g2s(st, p.atiles + ((size_t)w.mg * g.j + j) * kTcABytes, kTcABytes, &ld_full[s]);
+        else if (lane <= nvalid)
+          bulk_g2s(st + kTcABytes + kTcBBytes + (lane - 1) * 1024,
+                   p.field + (((size_t)w.t * g.v3 + s0 + (lane - 1)) * 256 + w.h * 128), 1024, &ld_full[s]);
+      }
+    }
+    if (!ok) {  // let the copies already issued land before the CTA exits
+      const uint32_t from = gi > (uint32_t)kTcStages ? gi - kTcStages : 0;
+      for (uint32_t k = from; k < gi; ++k) mbar_wait_bounded(&ld_full[k % kTcStages], (k / kTcStages) & 1, kWaitLimitNs / 8);
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer
+    uint32_t gi = 0, win = 0, buf = 0;
+    bool ok = true;
+    const uint32_t sbase = smem_addr(stages);
+    for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
+      const Unit w = decode(g, u);
+      const int n = w.j1 - w.j0;
+      for (int i = 0; i < n; ++i, ++gi) {
+        const int s = gi % kTcStages;
+        const bool wf = (i % kTcFlush) == 0, wl = (i % kTcFlush) == kTcFlush - 1 || i == n - 1;
+        bool okw = true;
+        if (wf) {
+          buf = win & 1;
+          if (win >= 2) okw = mbar_wait_bounded(&acc_empty[buf], ((win >> 1) - 1) & 1, kWaitLimitNs);
+        }
+        okw = okw && mbar_wait_bounded(&op_full[s], (gi / kTcStages) & 1, kWaitLimitNs);
+        ok = __all_sync(0xffffffffu, okw) && !*abort_flag;
+        if (!ok) {
+          if (lane == 0) tc_abort(abort_flag, p.status, 0x200000u | (unsigned)u);
+          break;
+        }
+        tc_fence_after();
+        if (lane == 0) {
+          const uint32_t st = sbase + s * kTcStageBytes;
+          const uint64_t bh = umma_desc(st + kTcABytes, kTcLbo, kTcSbo);
+          const uint64_t bl = umma_desc(st + kTcABytes + 4096, kTcLbo, kTcSbo);
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt) {
+            const uint64_t ah = umma_desc(st + mt * 8192, kTcLbo, kTcSbo);
+            const uint64_t al = umma_desc(st + mt * 8192 + 4096, kTcLbo, kTcSbo);
+            const uint32_t d = tmem + buf * 256 + mt * 128;
+            umma_bf16(d, ah, bh, kTcIdesc, wf ? 0u : 1u);
+            umma_bf16(d, ah, bl, kTcIdesc, 1u);
+            umma_bf16(d, al, bh, kTcIdesc, 1u);
+          }
+          umma_commit(&op_empty[s]);
+          if (wl) umma_commit(&acc_full[buf]);
+        }
+        __syncwarp();
+        if (wl) ++win;
+      }
+    }
+    // every MMA issued by this CTA completes before TMEM is released
+    if (lane == 0) umma_commit(fin);
+    __syncwarp();
+    mbar_wait_bounded(fin, 0, kWaitLimitNs);
+  } else {
+    // ---------------------------------------- convert + accumulate + store
+    const int wi = warp - 2;
+    const int q = warp & 3, mt = wi >> 2, row = 32 * q + lane;  // TMEM lane quarter of this warp
+    const int pair = (wi & 3) * 32 + lane, sh = wi >> 2;        // conversion: pair, sites 4sh..4sh+3
+    float run[128];
+#pragma unroll
+    for (int k = 0; k < 128; ++k) run[k] = 0.f;
+    uint32_t gi = 0, win = 0;
+    int pend = -1, pend_unit = -1;
+    bool pend_last = false, ok = true;
+
+    auto flush = [&](int wdx) -> bool {
+      const uint32_t b = wdx & 1;
+      const bool okw = __all_sync(0xffffffffu, mbar_wait_bounded(&acc_full[b], (wdx >> 1) & 1, kWaitLimitNs));
+      if (!okw || *abort_flag) return false;
+      tc_fence_after();
+      const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + b * 256 + mt * 128;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        float v[16];
+        tmem_ld16(base + 16 * k, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) run[16 * k + i] += v[i];
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
+      return true;
+    };
+    auto store = [&](int unit) {
+      float4 *dst = reinterpret_cast<float4 *>(p.partial + (((size_t)unit * 2 + mt) * 128 + row) * 128);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        dst[k] = make_float4(run[4 * k], run[4 * k + 1], run[4 * k + 2], run[4 * k + 3]);
+        run[4 * k] = run[4 * k + 1] = run[4 * k + 2] = run[4 * k + 3] = 0.f;
+      }
+    };
+
+    for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
+      const Unit w = decode(g, u);
+      const int n = w.j1 - w.j0;
+      for (int i = 0; i < n; ++i, ++gi) {
+        const int s = gi % kTcStages;
+        ok = __all_sync(0xffffffffu, mbar_wait_bounded(&ld_full[s], (gi / kTcStages) & 1, kWaitLimitNs)) &&
+             !*abort_flag;
+        if (!ok) {
+          if (lane == 0) tc_abort(abort_flag, p.status, 0x300000u | (unsigned)u);
+          break;
+        }
+        unsigned char *st = stages + s * kTcStageBytes;
+        const long long s0 = (long long)(w.j0 + i) * 8;
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int s8 = sh * 4 + k;
+          float2 c = make_float2(0.f, 0.f);
+          if (s0 + s8 < g.v3) c = reinterpret_cast<const float2 *>(st + kTcABytes + kTcBBytes + s8 * 1024)[pair];
+          split2(c.x, c.y, hi[k], lo[k]);
+        }
+        const uint32_t off = (sh * 16 + (pair >> 3)) * 128 + (pair & 7) * 16;
+        *reinterpret_cast<uint4 *>(st + kTcABytes + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4 *>(st + kTcABytes + 4096 + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&op_full[s]);
+        if ((i % kTcFlush) == kTcFlush - 1 || i == n - 1) {
+          if (pend >= 0) {
+            if (!flush(pend)) {
+              ok = false;
+              if (lane == 0) tc_abort(abort_flag, p.status, 0x400000u | (unsigned)u);
+              break;
+            }
+            if (pend_last) store(pend_unit);
+          }
+          pend = (int)win++;
+          pend_unit = u;
+          pend_last = i == n - 1;
+        }
+      }
+    }
+    if (ok && pend >= 0) {
+      if (flush(pend)) {
+        if (pend_last) store(pend_unit);
+      } else if (lane == 0) {
+        tc_abort(abort_flag, p.status, 0x500000u);
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tmem, 512);
+}
+
+// Phase tiles: for momentum group mg and k-step j, the two 128-row m-tiles
+// (64 momenta x {Re, Im} rows each) over the 8 sites of the step, bf16 hi and
+// lo, in the K-major core-matrix layout.  Phi = ex * ey * ez in FP64 from the
+// FP64 tables exp(2 pi i k / L), k = (n * x) mod L exactly.
+__global__ void __launch_bounds__(256) momentum_phase_tiles(unsigned char *__restrict__ atiles,
+                                                            const __grid_constant__ MomPlan plan, long long v3, int nj)
+{
+  const int j = blockIdx.x, mg = blockIdx.y;
+  const int mt = threadIdx.x >> 7, r = threadIdx.x & 127;
+  const int pm = mg * 128 + mt * 64 + (r >> 1), comp = r & 1;
+  const int lx = plan.latt[0], ly = plan.latt[1], lz = plan.latt[2];
+  const bool live = pm < plan.np;
+  int nx = 0, ny = 0, nz = 0;
+  if (live) {
+    const int qq = plan.p_q[pm];
+    nx = plan.px[plan.q_ix[qq]];
+    ny = plan.q_ny[qq];
+    nz = plan.p_nz[pm];
+  }
+  uint32_t w[2][2][4];
+#pragma unroll
+  for (int s8 = 0; s8 < 8; ++s8) {
+    const long long s = (long long)j * 8 + s8;
+    double re = 0.0, im = 0.0;
+    if (live && s < v3) {
+      const int x = (int)(s % lx);
+      const long long r2 = s / lx;
+      const int y = (int)(r2 % ly), z = (int)(r2 / ly);
+      const int kx = ((nx * x) % lx + lx) % lx, ky = ((ny * y) % ly + ly) % ly, kz = ((nz * z) % lz + lz) % lz;
+      const double axr = plan.cosx[kx], axi = plan.sinx[kx], ayr = plan.cosy[ky], ayi = plan.siny[ky];
+      const double azr = plan.cosz[kz], azi = plan.sinz[kz];
+      const double xyr = axr * ayr - axi * ayi, xyi = axr * ayi + axi * ayr;
+      re = xyr * azr - xyi * azi;
+      im = xyr * azi + xyi * azr;
+    }
+    const double a0 = comp ? im : re, a1 = comp ? re : -im;  // columns 2s (Re C) and 2s+1 (Im C)
+    const __nv_bfloat162 h = __floats2bfloat162_rn((float)a0, (float)a1);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn((float)(a0 - (double)hf.x), (float)(a1 - (double)hf.y));
+    w[s8 >> 2][0][s8 & 3] = bf16x2_bits(h);
+    w[s8 >> 2][1][s8 & 3] = bf16x2_bits(l);
+  }
+  unsigned char *tile = atiles + (((size_t)mg * nj + j) * 4 + mt * 2) * 4096;
+#pragma unroll
+  for (int kc = 0; kc < 2; ++kc) {
+    const uint32_t off = (kc * 16 + (r >> 3)) * 128 + (r & 7) * 16;
+    *reinterpret_cast<uint4 *>(tile + off) = make_uint4(w[kc][0][0], w[kc][0][1], w[kc][0][2], w[kc][0][3]);
+    *reinterpret_cast<uint4 *>(tile + 4096 + off) = make_uint4(w[kc][1][0], w[kc][1][1], w[kc][1][2], w[kc][1][3]);
+  }
+}
+
+// out[p][t][n] = sum over the k-blocks of the unit partials, FP64, fixed order.
+__global__ void __launch_bounds__(256) momentum_tc_reduce(const float *__restrict__ partial, double2 *__restrict__ out,
+                                                          const __grid_constant__ TcGeom g, int np)
+{
+  const int pm = blockIdx.x, t = blockIdx.y, n = threadIdx.x;
+  if (pm >= np) return;
+  const int mg = pm >> 7, pr = pm & 127, mt = pr >> 6, pp = pr & 63, h = n >> 7, col = n & 127;
+  double re = 0.0, im = 0.0;
+  for (int jb = 0; jb < g.jb; ++jb) {
+    const long long u = ((long long)(mg * g.jb + jb) * g.lt + t) * 2 + h;
+    const float *b = partial + ((size_t)u * 2 + mt) * 128 * 128;
+    re += (double)b[(2 * pp) * 128 + col];
+    im += (double)b[(2 * pp + 1) * 128 + col];
+  }
+  out[((size_t)pm * g.lt + t) * 256 + n] = make_double2(re, im);
+}
+
+} // namespace
+
+TcGeom make_tc_geom(const MomPlan &plan)
+{
+  TcGeom g {};
+  g.v3 = (long long)plan.latt[0] * plan.latt[1] * plan.latt[2];
+  g.lt = plan.latt[3];
+  g.j = (int)((g.v3 + 7) / 8);
+  g.ku = g.j < kTcUnitSteps ? g.j : kTcUnitSteps;
+  g.jb = (g.j + g.ku - 1) / g.ku;
+  g.mg = (plan.np + 127) / 128;
+  g.units = g.mg * g.jb * g.lt * 2;
+  return g;
+}
+
+size_t tc_phase_bytes(const TcGeom &g) { return (size_t)g.mg * g.j * kTcABytes; }
+size_t tc_partial_bytes(const TcGeom &g) { return (size_t)g.units * 2 * 128 * 128 * sizeof(float); }
+
+cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom &g, const void *field,
+                               unsigned char *atiles, float *partial, void *out)
+{
+  static bool attr_set[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 64 && !attr_set[dev]) {
+    e = cudaFuncSetAttribute(momentum_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (e != cudaSuccess) return e;
+    attr_set[dev] = true;
+  }
+  momentum_phase_tiles<<<dim3(g.j, g.mg), 256, 0, job.stream>>>(atiles, plan, g.v3, g.j);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  TcParams tp;
+  tp.field = static_cast<const float2 *>(field);
+  tp.atiles = atiles;
+  tp.partial = partial;
+  tp.status = job.status;
+  tp.g = g;
+  const int grid = g.units < job.num_sms ? g.units : job.num_sms;
+  momentum_gemm_tc<<<grid, kTcThreads, kTcSmem, job.stream>>>(tp);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  momentum_tc_reduce<<<dim3(plan.np, g.lt), 256, 0, job.stream>>>(partial, static_cast<double2 *>(out), g, plan.np);
+  return cudaGetLastError();
+}
+
+} // namespace cgb

@@ -22,8 +22,29 @@ struct MomPlan {
   double cosz[kMomMaxL], sinz[kMomMaxL];
 };
 
+// Geometry of the tensor-core projection (kernels_momentum_tc.cu): k-steps of
+// 8 sites per timeslice, k-steps per work unit, units.
+constexpr int kTcUnitSteps = 256;
+struct TcGeom {
+  long long v3;  // sites per timeslice
+  int lt;        // timeslices
+  int j;         // k-steps per timeslice, ceil(v3 / 8)
+  int ku;        // k-steps per unit
+  int jb;        // units per (momentum group, t, pair half)
+  int mg;        // momentum groups of 128
+  int units;     // mg * jb * lt * 2
+};
+TcGeom make_tc_geom(const MomPlan &plan);
+size_t tc_phase_bytes(const TcGeom &g);
+size_t tc_partial_bytes(const TcGeom &g);
+cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom &g, const void *field,
+                               unsigned char *atiles, float *partial, void *out);
+
 // All-gamma meson correlators at the plan's momenta: out[p][t][16*16]
-// complex128 (device).  Uses job.ws for the per-site values and plane sums.
-cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out);
+// complex128 (device).  Uses job.ws for the per-site values and the plane
+// sums, or (tensor_cores, complex64 only) the phase tiles and unit partials
+// of the tensor-core projection.
+cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out,
+                                  bool tensor_cores = false);
 
 } // namespace cgb

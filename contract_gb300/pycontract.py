@@ -60,6 +60,7 @@ class BaryonSequentialType(enum.IntEnum):
 
 CONTRACT_C128 = 0
 CONTRACT_C64 = 1
+CONTRACT_C64_TC = 2  # momentum projection on the tensor cores (split bf16)
 _ERRORS_RECORD = 1
 
 

@@ -30,6 +30,11 @@ extern "C" {
 enum {
   CONTRACT_C128 = 0,
   CONTRACT_C64 = 1,
+  /* contract_meson_all_gamma_momentum only: complex64 propagators, FP32
+   * site arithmetic, and the projection as a tensor-core GEMM with each
+   * operand split into two bf16 terms (hi*hi + hi*lo + lo*hi), FP32
+   * accumulation and an FP64 sum per timeslice. */
+  CONTRACT_C64_TC = 2,
 };
 
 /* ----------------------------------------------------------- errors ---- */
@@ -163,7 +168,9 @@ void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int n
  * moms: HOST int[nmom][3] = (nx, ny, nz); lattice required, spatial extents
  * <= 64, at most 8 distinct nx and 128 distinct (nx, ny) per call.  correl:
  * device complex128 [nmom][Lt][256].  Uses the per-device workspace for
- * V x 256 site values and the per-plane partial sums (FP64). */
+ * V x 256 site values and the per-plane partial sums (FP64), or with
+ * CONTRACT_C64_TC the bf16 phase tiles and the FP32 partials of the
+ * tensor-core projection. */
 void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const void *propag_j, size_t volume,
                                        const int *lattice, const int *moms, int nmom, int precision);
 

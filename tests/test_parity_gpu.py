@@ -15,6 +15,11 @@ TOL_C128 = 1e-12           # plain form (FP64 throughout)
 # relative bound; with the i.i.d. Gaussian test propagators every timeslice is
 # a zero-mean random walk of site values, and sigma_t is its natural scale.
 TOL_C64_TIMESLICE = 1e-6
+# Tensor-core momentum projection (CONTRACT_C64_TC): each operand is split
+# into two bf16 terms and the hi*lo' products are kept (the lo*lo' term and the
+# second-order split residuals, each <= 2^-18 relative, are dropped), with
+# FP32 accumulation; the error bound is relative to max(|C_t|, sigma_t).
+TOL_C64_TC = 3e-5
 
 LATT = (4, 4, 4, 8)
 
@@ -181,7 +186,7 @@ def test_autotuned_variants_agree(api, props, c_oracle):
     assert lib.contract_autotune_report(buf, len(buf)) >= 2
 
 
-@pytest.mark.parametrize("latt", [(4, 4, 4, 4), (6, 2, 4, 3)])
+@pytest.mark.parametrize("latt", [(4, 4, 4, 4), (6, 2, 4, 3), (2, 3, 3, 2)])
 def test_meson_all_gamma_momentum(api, latt, c_oracle):
     """All 16 x 16 meson pairs projected to momenta, both precisions, against
     the FP64 oracle (per-site all-gamma values, then the explicit phase sum)."""
@@ -199,9 +204,11 @@ def test_meson_all_gamma_momentum(api, latt, c_oracle):
     v = pi.shape[0]
     lat = (ctypes.c_int * 4)(*latt)
     m = np.ascontiguousarray(moms.astype(np.int32))
-    for prec in (0, 1):
+    # sigma per (p, t, gamma pair): root-sum-square of the site terms
+    sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real).T[None]  # [1, Lt, 256]
+    for prec in (0, 1, 2):
         out = torch.full((len(moms), latt[3], 256), float("nan"), dtype=torch.complex128, device="cuda")
-        a, b = cuda(pi, prec == 1), cuda(pj, prec == 1)
+        a, b = cuda(pi, prec >= 1), cuda(pj, prec >= 1)
         lib.contract_meson_all_gamma_momentum(out.data_ptr(), a.data_ptr(), b.data_ptr(), v, lat,
                                               m.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(moms), prec)
         got = out.cpu().numpy()
@@ -209,11 +216,38 @@ def test_meson_all_gamma_momentum(api, latt, c_oracle):
         if prec == 0:
             assert rel_err(got, ref) < TOL_C128
         else:
-            # sigma per (p, t, gamma pair): root-sum-square of the site terms
-            x, y, z, t = eo.eo_coords(latt)
-            sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real).T[None]  # [1, Lt, 256]
             err = np.abs(got - ref) / np.maximum(np.abs(ref), sig)
-            assert err.max() < TOL_C64_TIMESLICE
+            assert err.max() < (TOL_C64_TIMESLICE if prec == 1 else TOL_C64_TC)
+    api.check_device()
+
+
+def test_momentum_tensor_cores_two_momentum_groups(api):
+    """CONTRACT_C64_TC with 147 momenta (two groups of 128 GEMM rows) on a
+    lattice whose timeslice (6 x 6 x 4 = 144 sites) spans 18 k-steps."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    latt = (6, 6, 4, 2)
+    pi = eo.make_propagator(latt, 41, 0.2)
+    pj = eo.make_propagator(latt, 42, 0.3)
+    r3, r1 = np.arange(-3, 4), np.arange(-1, 2)
+    moms = np.stack(np.meshgrid(r3, r3, r1, indexing="ij"), -1).reshape(-1, 3)
+    assert len(moms) == 147
+    site = eo.meson_all_gamma(pi, pj).reshape(256, -1)
+    ref = eo.momentum_project(site, latt, moms).transpose(1, 2, 0)
+    sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real).T[None]
+    out = torch.full((len(moms), latt[3], 256), float("nan"), dtype=torch.complex128, device="cuda")
+    m = np.ascontiguousarray(moms.astype(np.int32))
+    a, b = cuda(pi, True), cuda(pj, True)  # keep both alive across the call
+    lib.contract_meson_all_gamma_momentum(out.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                          pi.shape[0], (ctypes.c_int * 4)(*latt),
+                                          m.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(moms), 2)
+    got = out.cpu().numpy()
+    assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+    err = np.abs(got - ref) / np.maximum(np.abs(ref), sig)
+    assert err.max() < TOL_C64_TC
+    api.check_device()
 
 
 BATCH_LATTS = [(4, 4, 4, 8), (4, 2, 2, 6), (6, 4, 2, 4), (2, 2, 2, 2)]
