@@ -16,17 +16,20 @@
 // Work: units (momentum group of 128, block of k-steps, t, pair half) are
 // dealt round-robin to persistent CTAs, so the CTAs running together share
 // the same phase tiles (L2-resident; the phase matrix does not depend on t).
-// Roles in a CTA (320 threads):
-//   warp 0     TMA producer: per k-step one 16 KB phase tile (both m-tiles,
-//              hi and lo, pre-tiled in global memory) and up to eight 1 KB
-//              rows of the complex64 per-site field into a staging buffer
+// Roles in a CTA (352 threads):
+//   warp 0     bulk copies of up to eight 1 KB rows of the complex64 per-site
+//              field per k-step into a 10-deep staging ring (HBM latency)
+//   warp 10    bulk copies of the 16 KB phase tile per k-step (both m-tiles,
+//              hi and lo, pre-tiled in global memory) into a 5-deep operand ring
 //   warp 1     allocates the 512 TMEM columns and issues the MMAs: for each
 //              of the two 128-row m-tiles three M=128, N=128, K=16 MMAs per
 //              k-step, into one of two accumulator buffers
-//   warps 2-9  convert the staged FP32 values into the bf16 hi/lo operand
-//              tiles, and every kTcFlush k-steps move an accumulator buffer
-//              into FP32 registers (tcgen05.ld) and release it; at the end
-//              of a unit they store its 256 x 128 FP32 partial
+//   warps 2-9  convert the staged FP32 values into the bf16 hi/lo field tile
+//              of the operand ring (four groups of two warps, each taking every
+//              fourth k-step), and all eight drain each accumulator buffer
+//              (kTcFlush k-steps of MMAs) into FP32 registers (tcgen05.ld) a
+//              few k-steps after its window ends, releasing it; at the end of
+//              a unit they store its 256 x 128 FP32 partial
 // A final kernel sums the partials of each (t, p, n) in FP64 in a fixed order.
 // Every mbarrier wait is bounded; on a timeout the CTA stops, reports
 // kDevErrWaitTimeout, waits (bounded) for its copies and MMAs and frees TMEM.
@@ -40,15 +43,18 @@ namespace cgb {
 
 namespace {
 
-constexpr int kTcStages = 6;
-constexpr int kTcFlush = 4;       // k-steps per accumulator buffer
-constexpr int kTcThreads = 320;
+constexpr int kTcOpStages = 5;    // operand ring: phase tile + converted field tile
+constexpr int kTcStgStages = 10;  // staging ring: complex64 field rows (HBM latency)
+constexpr int kTcFlush = 8;       // k-steps per accumulator buffer
+constexpr int kTcGroups = 4;      // converter groups of two warps, one k-step each in turn
+constexpr int kTcDrainLag = 3;    // k-steps converted past a window's end before draining it (< kTcOpStages)
+constexpr int kTcThreads = 352;   // 11 warps
 constexpr int kTcHeader = 1024;   // barriers, TMEM slot, abort flag
 constexpr int kTcABytes = 16384;  // 2 m-tiles x {hi, lo} x 128 x 16 bf16
 constexpr int kTcBBytes = 8192;   // {hi, lo} x 128 x 16 bf16
+constexpr int kTcOpBytes = kTcABytes + kTcBBytes;
 constexpr int kTcStgBytes = 8192; // 8 sites x 128 pairs x complex64
-constexpr int kTcStageBytes = kTcABytes + kTcBBytes + kTcStgBytes;
-constexpr int kTcSmem = kTcHeader + kTcStages * kTcStageBytes;
+constexpr int kTcSmem = kTcHeader + kTcOpStages * kTcOpBytes + kTcStgStages * kTcStgBytes;
 constexpr uint32_t kTcIdesc = umma_idesc_bf16(128, 128);
 constexpr uint32_t kTcLbo = 16 * 128, kTcSbo = 128;  // 128-row tiles
 
@@ -98,22 +104,29 @@ __device__ __forceinline__ void tc_abort(volatile int *abort_flag, DeviceStatus 
 __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_constant__ TcParams p)
 {
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t *ld_full = reinterpret_cast<uint64_t *>(smem);
-  uint64_t *op_full = ld_full + kTcStages;
-  uint64_t *op_empty = op_full + kTcStages;
-  uint64_t *acc_full = op_empty + kTcStages;
+  uint64_t *stg_full = reinterpret_cast<uint64_t *>(smem);
+  uint64_t *stg_empty = stg_full + kTcStgStages;
+  uint64_t *a_full = stg_empty + kTcStgStages;
+  uint64_t *op_full = a_full + kTcOpStages;
+  uint64_t *op_empty = op_full + kTcOpStages;
+  uint64_t *acc_full = op_empty + kTcOpStages;
   uint64_t *acc_empty = acc_full + 2;
   uint64_t *fin = acc_empty + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 512);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 516);
-  unsigned char *stages = smem + kTcHeader;
+  unsigned char *ops = smem + kTcHeader;
+  unsigned char *stgs = ops + kTcOpStages * kTcOpBytes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const TcGeom &g = p.g;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kTcStages; ++s) {
-      mbar_init(&ld_full[s], 1);
-      mbar_init(&op_full[s], 8);
+    for (int s = 0; s < kTcStgStages; ++s) {
+      mbar_init(&stg_full[s], 1);
+      mbar_init(&stg_empty[s], 8 / kTcGroups);
+    }
+    for (int s = 0; s < kTcOpStages; ++s) {
+      mbar_init(&a_full[s], 1);
+      mbar_init(&op_full[s], 8 / kTcGroups);
       mbar_init(&op_empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -133,18 +146,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
-    // ------------------------------------------------------- TMA producer
+  if (warp == 0 || warp == 10) {
+    // ------------------------------------------- bulk-copy producers
+    // warp 0: field rows into the staging ring (released by the converters);
+    // warp 10: phase tiles into the operand ring (released by MMA completion).
+    const bool field = warp == 0;
+    const int nst = field ? kTcStgStages : kTcOpStages;
+    uint64_t *full = field ? stg_full : a_full;
+    uint64_t *empty = field ? stg_empty : op_empty;
     uint32_t gi = 0;
     bool ok = true;
     for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
       const Unit w = decode(g, u);
       for (int j = w.j0; j < w.j1; ++j, ++gi) {
-        const int s = gi % kTcStages;
-        if (gi >= kTcStages) {
-          ok = __all_sync(0xffffffffu, mbar_wait_bounded(&op_empty[s], ((gi / kTcStages) - 1) & 1, kWaitLimitNs));
+        const int s = gi % nst;
+        if (gi >= (uint32_t)nst) {
+          ok = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], ((gi / nst) - 1) & 1, kWaitLimitNs));
           if (!ok) {
-            if (lane == 0) tc_abort(abort_flag, p.status, 0x100000u | (unsigned)u);
+            if (lane == 0) tc_abort(abort_flag, p.status, (field ? 0x100000u : 0x600000u) | (unsigned)u);
             break;
           }
         }
@@ -152,39 +171,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
           ok = false;
           break;
         }
-        const long long s0 = (long long)j * 8;
-        const int nvalid = (int)min(8LL, g.v3 - s0);
-        unsigned char *st = stages + s * kTcStageBytes;
-        if (lane == 0) mbar_arrive_expect_tx(&ld_full[s], (uint32_t)(kTcABytes + nvalid * 1024));
-        __syncwarp();
-        if (lane == 0)
-          bulk_g2s(st, p.atiles + ((size_t)w.mg * g.j + j) * kTcABytes, kTcABytes, &ld_full[s]);
-        else if (lane <= nvalid)
-          bulk_g2s(st + kTcABytes + kTcBBytes + (lane - 1) * 1024,
-                   p.field + (((size_t)w.t * g.v3 + s0 + (lane - 1)) * 256 + w.h * 128), 1024, &ld_full[s]);
+        if (field) {
+          const long long s0 = (long long)j * 8;
+          const int nvalid = (int)min(8LL, g.v3 - s0);
+          unsigned char *st = stgs + s * kTcStgBytes;
+          if (lane == 0) mbar_arrive_expect_tx(&full[s], (uint32_t)(nvalid * 1024));
+          __syncwarp();
+          if (lane < nvalid)
+            bulk_g2s(st + lane * 1024, p.field + (((size_t)w.t * g.v3 + s0 + lane) * 256 + w.h * 128), 1024,
+                     &full[s]);
+        } else if (lane == 0) {
+          mbar_arrive_expect_tx(&full[s], (uint32_t)kTcABytes);
+          bulk_g2s(ops + s * kTcOpBytes, p.atiles + ((size_t)w.mg * g.j + j) * kTcABytes, kTcABytes, &full[s]);
+        }
       }
     }
     if (!ok) {  // let the copies already issued land before the CTA exits
-      const uint32_t from = gi > (uint32_t)kTcStages ? gi - kTcStages : 0;
-      for (uint32_t k = from; k < gi; ++k) mbar_wait_bounded(&ld_full[k % kTcStages], (k / kTcStages) & 1, kWaitLimitNs / 8);
+      const uint32_t from = gi > (uint32_t)nst ? gi - nst : 0;
+      for (uint32_t k = from; k < gi; ++k) mbar_wait_bounded(&full[k % nst], (k / nst) & 1, kWaitLimitNs / 8);
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
     uint32_t gi = 0, win = 0, buf = 0;
     bool ok = true;
-    const uint32_t sbase = smem_addr(stages);
+    const uint32_t sbase = smem_addr(ops);
     for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
       const Unit w = decode(g, u);
       const int n = w.j1 - w.j0;
       for (int i = 0; i < n; ++i, ++gi) {
-        const int s = gi % kTcStages;
+        const int s = gi % kTcOpStages;
         const bool wf = (i % kTcFlush) == 0, wl = (i % kTcFlush) == kTcFlush - 1 || i == n - 1;
         bool okw = true;
         if (wf) {
           buf = win & 1;
           if (win >= 2) okw = mbar_wait_bounded(&acc_empty[buf], ((win >> 1) - 1) & 1, kWaitLimitNs);
         }
-        okw = okw && mbar_wait_bounded(&op_full[s], (gi / kTcStages) & 1, kWaitLimitNs);
+        okw = okw && mbar_wait_bounded(&a_full[s], (gi / kTcOpStages) & 1, kWaitLimitNs);
+        okw = okw && mbar_wait_bounded(&op_full[s], (gi / kTcOpStages) & 1, kWaitLimitNs);
         ok = __all_sync(0xffffffffu, okw) && !*abort_flag;
         if (!ok) {
           if (lane == 0) tc_abort(abort_flag, p.status, 0x200000u | (unsigned)u);
@@ -192,7 +215,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
         }
         tc_fence_after();
         if (lane == 0) {
-          const uint32_t st = sbase + s * kTcStageBytes;
+          const uint32_t st = sbase + s * kTcOpBytes;
           const uint64_t bh = umma_desc(st + kTcABytes, kTcLbo, kTcSbo);
           const uint64_t bl = umma_desc(st + kTcABytes + 4096, kTcLbo, kTcSbo);
 #pragma unroll
@@ -219,13 +242,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
     // ---------------------------------------- convert + accumulate + store
     const int wi = warp - 2;
     const int q = warp & 3, mt = wi >> 2, row = 32 * q + lane;  // TMEM lane quarter of this warp
-    const int pair = (wi & 3) * 32 + lane, sh = wi >> 2;        // conversion: pair, sites 4sh..4sh+3
+    // conversion: group gp converts every kTcGroups-th k-step; its 64 threads
+    // take pairs t64 and t64 + 64 over all 8 sites of the step
+    const int gp = wi >> 1, t64 = ((wi & 1) << 5) | lane;
     float run[128];
 #pragma unroll
     for (int k = 0; k < 128; ++k) run[k] = 0.f;
     uint32_t gi = 0, win = 0;
-    int pend = -1, pend_unit = -1;
-    bool pend_last = false, ok = true;
+    // Windows whose MMAs are issued but not yet drained (at most two, one per
+    // accumulator buffer): window index, unit, last window of the unit, and
+    // the k-step that ended it.
+    int nq = 0, qw0 = 0, qw1 = 0, qu0 = 0, qu1 = 0;
+    bool ql0 = false, ql1 = false;
+    uint32_t qe0 = 0, qe1 = 0;
+    bool ok = true;
 
     auto flush = [&](int wdx) -> bool {
       const uint32_t b = wdx & 1;
@@ -234,11 +264,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
       tc_fence_after();
       const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + b * 256 + mt * 128;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        float v[16];
-        tmem_ld16(base + 16 * k, v);
+      for (int k = 0; k < 4; ++k) {
+        float v[32];
+        tmem_ld32(base + 32 * k, v);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) run[16 * k + i] += v[i];
+        for (int i = 0; i < 32; ++i) run[32 * k + i] += v[i];
       }
       tc_fence_before();
       __syncwarp();
@@ -253,54 +283,94 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
         run[4 * k] = run[4 * k + 1] = run[4 * k + 2] = run[4 * k + 3] = 0.f;
       }
     };
+    // Drain the oldest pending window: its accumulator into `run`, and the
+    // unit's partial when it was the unit's last window.
+    auto drain_front = [&]() -> bool {
+      if (!flush(qw0)) return false;
+      if (ql0) store(qu0);
+      qw0 = qw1;
+      qu0 = qu1;
+      ql0 = ql1;
+      qe0 = qe1;
+      --nq;
+      return true;
+    };
 
     for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
       const Unit w = decode(g, u);
       const int n = w.j1 - w.j0;
       for (int i = 0; i < n; ++i, ++gi) {
-        const int s = gi % kTcStages;
-        ok = __all_sync(0xffffffffu, mbar_wait_bounded(&ld_full[s], (gi / kTcStages) & 1, kWaitLimitNs)) &&
-             !*abort_flag;
-        if (!ok) {
-          if (lane == 0) tc_abort(abort_flag, p.status, 0x300000u | (unsigned)u);
-          break;
-        }
-        unsigned char *st = stages + s * kTcStageBytes;
-        const long long s0 = (long long)(w.j0 + i) * 8;
-        uint32_t hi[4], lo[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int s8 = sh * 4 + k;
-          float2 c = make_float2(0.f, 0.f);
-          if (s0 + s8 < g.v3) c = reinterpret_cast<const float2 *>(st + kTcABytes + kTcBBytes + s8 * 1024)[pair];
-          split2(c.x, c.y, hi[k], lo[k]);
-        }
-        const uint32_t off = (sh * 16 + (pair >> 3)) * 128 + (pair & 7) * 16;
-        *reinterpret_cast<uint4 *>(st + kTcABytes + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4 *>(st + kTcABytes + 4096 + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-        fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&op_full[s]);
-        if ((i % kTcFlush) == kTcFlush - 1 || i == n - 1) {
-          if (pend >= 0) {
-            if (!flush(pend)) {
-              ok = false;
-              if (lane == 0) tc_abort(abort_flag, p.status, 0x400000u | (unsigned)u);
-              break;
-            }
-            if (pend_last) store(pend_unit);
+        if ((int)(gi % kTcGroups) == gp) {
+          const int ss = gi % kTcStgStages, so = gi % kTcOpStages;
+          bool okw = mbar_wait_bounded(&stg_full[ss], (gi / kTcStgStages) & 1, kWaitLimitNs);
+          // the operand slot's field tile is free once the MMAs of k-step gi - kTcOpStages completed
+          if (gi >= (uint32_t)kTcOpStages)
+            okw = okw && mbar_wait_bounded(&op_empty[so], ((gi / kTcOpStages) - 1) & 1, kWaitLimitNs);
+          ok = __all_sync(0xffffffffu, okw) && !*abort_flag;
+          if (!ok) {
+            if (lane == 0) tc_abort(abort_flag, p.status, 0x300000u | (unsigned)u);
+            break;
           }
-          pend = (int)win++;
-          pend_unit = u;
-          pend_last = i == n - 1;
+          const unsigned char *stg = stgs + ss * kTcStgBytes;
+          unsigned char *bt = ops + so * kTcOpBytes + kTcABytes;
+          const long long s0 = (long long)(w.j0 + i) * 8;
+#pragma unroll
+          for (int pp = 0; pp < 2; ++pp) {
+            const int pair = t64 + 64 * pp;
+#pragma unroll
+            for (int sh = 0; sh < 2; ++sh) {
+              uint32_t hi[4], lo[4];
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                const int s8 = sh * 4 + k;
+                float2 c = make_float2(0.f, 0.f);
+                if (s0 + s8 < g.v3) c = reinterpret_cast<const float2 *>(stg + s8 * 1024)[pair];
+                split2(c.x, c.y, hi[k], lo[k]);
+              }
+              const uint32_t off = (sh * 16 + (pair >> 3)) * 128 + (pair & 7) * 16;
+              *reinterpret_cast<uint4 *>(bt + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+              *reinterpret_cast<uint4 *>(bt + 4096 + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+            }
+          }
+          fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive(&stg_empty[ss]);
+            mbar_arrive(&op_full[so]);
+          }
+        }
+        if ((i % kTcFlush) == kTcFlush - 1 || i == n - 1) {  // this k-step ends a window
+          if (nq == 0) {
+            qw0 = (int)win++;
+            qu0 = u;
+            ql0 = i == n - 1;
+            qe0 = gi;
+          } else {
+            qw1 = (int)win++;
+            qu1 = u;
+            ql1 = i == n - 1;
+            qe1 = gi;
+          }
+          ++nq;
+        }
+        // Drain a window once kTcDrainLag more k-steps are converted (the MMAs
+        // have then caught up with it), or at once when both buffers are pending.
+        while (nq > 0 && (nq == 2 || gi - qe0 >= (uint32_t)kTcDrainLag)) {
+          if (!drain_front()) {
+            ok = false;
+            break;
+          }
+        }
+        if (!ok) {
+          if (lane == 0) tc_abort(abort_flag, p.status, 0x400000u | (unsigned)u);
+          break;
         }
       }
     }
-    if (ok && pend >= 0) {
-      if (flush(pend)) {
-        if (pend_last) store(pend_unit);
-      } else if (lane == 0) {
-        tc_abort(abort_flag, p.status, 0x500000u);
+    while (ok && nq > 0) {
+      if (!drain_front()) {
+        ok = false;
+        if (lane == 0) tc_abort(abort_flag, p.status, 0x500000u);
       }
     }
   }
