@@ -41,9 +41,11 @@ GAMMA_CG5 = 5
 N_TYPES = 6
 N_PROJ = 2
 UNITS_PER_SITE = N_TYPES * N_PROJ
-# FP32 operations per site of the fused kernel (loop form 576 complex FMA
-# + 2 triangles x 2 projectors x 2448 complex FMA + projector/Q set-up), 8 flops per complex FMA.
-FUSED_CFMA_PER_SITE = 576 + 4 * 2448 + 2 * 9 * 8
+# Complex FMAs per site executed by the fused kernel (16 threads per site, one (i, l) pair
+# each): loop form 36 (wedge) + 2 x 9 (dots with Q_w); each of the two triangle passes
+# 4 x 36 (wedges a ^ B_m) + 4 m x 2 basis terms x 9 (dots) + 8 x 2 (projector coefficients);
+# Q set-up 18 x 3.  8 flops per complex FMA.
+FUSED_CFMA_PER_SITE = 16 * (36 + 18) + 2 * 16 * (4 * 36 + 8 * 9 + 8 * 2) + 18 * 3
 WORKLOAD = "baryon_2pt_24c64"
 METRIC = "GSite/s & HBM GB/s: mixed vs FP64 GPU contraction at <=1e-6 rel err/timeslice"
 

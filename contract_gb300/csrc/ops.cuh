@@ -218,7 +218,7 @@ __device__ __forceinline__ void loop_site(const BaryonSpin<R> &b, const S *A, co
 
 // Triangle form over N' (NW slots of 144 complex).  Writes vals[v*NW + w].
 // Loop order l -> m -> w: each B block is loaded once and feeds every
-// projector's accumulator.
+// projector; with two projectors the wedge a ^ B_m is shared between them.
 template <class R, class S, int TPS, int NV, int NW>
 __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A, const S *B, const S *np, int sub,
                                               int c1sel, cx<R> *vals)
@@ -241,35 +241,71 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
 #pragma unroll
   for (int lo = 0; lo < Ln::LPT; ++lo) {
     const int l = l0 + lo;
-    cx<R> d[NW][9];
+    if constexpr (NW >= 2) {
+      // a . (B_m ^ N'_w) = N'_w . (a ^ B_m): one wedge per m shared by the projectors.
+      cx<R> a[9];
+      load9(a, A + (i * 4 + b.perm2[l]) * 9);
+      cx<R> sw[NW];
 #pragma unroll
-    for (int w = 0; w < NW; ++w)
-#pragma unroll
-      for (int k = 0; k < 9; ++k) d[w][k] = czero<R>();
-    // Not unrolled: keeps one B block and one N' block live (register pressure).
+      for (int w = 0; w < NW; ++w) sw[w] = czero<R>();
 #pragma unroll 1
-    for (int m = 0; m < 4; ++m) {
-      cx<R> bm[9];
-      if constexpr (kCacheB) {
+      for (int m = 0; m < 4; ++m) {
+        cx<R> e[9];
+        {
+          cx<R> bm[9];
+          if constexpr (kCacheB) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) bm[k] = brow[m][k];
-      } else {
-        load9(bm, B + (j * 4 + m) * 9);
+            for (int k = 0; k < 9; ++k) bm[k] = brow[m][k];
+          } else {
+            load9(bm, B + (j * 4 + m) * 9);
+          }
+#pragma unroll
+          for (int k = 0; k < 9; ++k) e[k] = czero<R>();
+          wedge_acc(e, a, bm);
+        }
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          cx<R> nn[9];
+          load9(nn, np + (size_t)w * 144 + (m * 4 + l) * 9);
+          const cx<R> t = dot9(nn, e);
+          sw[w] = cadd(sw[w], t);
+        }
       }
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(sw[w], b.ph2[v][l]));
+    } else {
+      cx<R> d[NW][9];
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) d[w][k] = czero<R>();
+      // Not unrolled: keeps one B block and one N' block live (register pressure).
+#pragma unroll 1
+      for (int m = 0; m < 4; ++m) {
+        cx<R> bm[9];
+        if constexpr (kCacheB) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) bm[k] = brow[m][k];
+        } else {
+          load9(bm, B + (j * 4 + m) * 9);
+        }
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          cx<R> nn[9];
+          load9(nn, np + (size_t)w * 144 + (m * 4 + l) * 9);
+          wedge_acc(d[w], bm, nn);
+        }
+      }
+      cx<R> a[9];
+      load9(a, A + (i * 4 + b.perm2[l]) * 9);
 #pragma unroll
       for (int w = 0; w < NW; ++w) {
-        cx<R> nn[9];
-        load9(nn, np + (size_t)w * 144 + (m * 4 + l) * 9);
-        wedge_acc(d[w], bm, nn);
+        const cx<R> s = dot9(a, d[w]);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(s, b.ph2[v][l]));
       }
-    }
-    cx<R> a[9];
-    load9(a, A + (i * 4 + b.perm2[l]) * 9);
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      const cx<R> s = dot9(a, d[w]);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) acc[v][w] = cadd(acc[v][w], mul_phase(s, b.ph2[v][l]));
     }
   }
   const uint32_t p1 = b.ph1[c1sel][i];
@@ -282,9 +318,9 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
 // Triangle form with the projectors in the gamma basis (CliffordSet):
 //   D_k = sum_m B[perm1 i][m] ^ (i^ph[k][m] N[perm[k][m]][l]),  s_k = A[i][perm2 l] . D_k
 //   vals[v*NW + w] = c1(i) sum_l c2_v(l) sum_k coef[w][k] s_k
-// The basis term k runs outermost so that one D accumulator is live: loading
-// each B block once per term costs less than the extra registers of holding
-// every term's D (which pushed the two-CTA configuration into spills).
+// With two or more basis terms the wedge a ^ B[perm1 i][m] is formed once
+// per m and dotted with each term's N block; with one term the basis term
+// runs outermost so that one D accumulator is live.
 template <class R, class S, int TPS, int NV, int NW>
 __device__ __forceinline__ void triangle_cliff_site(const BaryonSpin<R> &b, const S *A, const S *B, const S *N, int sub,
                                                     int c1sel, cx<R> *vals)
@@ -306,23 +342,48 @@ __device__ __forceinline__ void triangle_cliff_site(const BaryonSpin<R> &b, cons
     cx<R> u[NW];  // sum_k coef[w][k] s_k for this l
 #pragma unroll
     for (int w = 0; w < NW; ++w) u[w] = czero<R>();
-#pragma unroll 1
-    for (int k = 0; k < cl.ng; ++k) {
-      cx<R> d[9];
-#pragma unroll
-      for (int e = 0; e < 9; ++e) d[e] = czero<R>();
-      const bool phased = cl.has_phase[k];
+    if (cl.ng >= 2) {
+      // The triple product a . (b ^ n) is symmetric in a, b, n, so
+      // s_k = sum_m n_km . E_m with E_m = a ^ B[perm1 i][m] shared by every
+      // basis term: 4 wedges + 4 ng dots instead of 4 ng wedges + ng dots.
 #pragma unroll 1
       for (int m = 0; m < 4; ++m) {
-        cx<R> bm[9], nn[9];
-        load9(bm, B + (j * 4 + m) * 9);
-        load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
-        if (phased) phase9(nn, cl.ph[k][m]);
-        wedge_acc(d, bm, nn);
-      }
-      const cx<R> s = dot9(a, d);
+        cx<R> e[9];
+        {
+          cx<R> bm[9];
+          load9(bm, B + (j * 4 + m) * 9);
 #pragma unroll
-      for (int w = 0; w < NW; ++w) cfma(u[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s);
+          for (int q = 0; q < 9; ++q) e[q] = czero<R>();
+          wedge_acc(e, a, bm);
+        }
+#pragma unroll 1
+        for (int k = 0; k < cl.ng; ++k) {
+          cx<R> nn[9];
+          load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
+          const cx<R> s = mul_phase(dot9(nn, e), cl.ph[k][m]);
+#pragma unroll
+          for (int w = 0; w < NW; ++w) cfma(u[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s);
+        }
+      }
+    } else {
+#pragma unroll 1
+      for (int k = 0; k < cl.ng; ++k) {
+        cx<R> d[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) d[e] = czero<R>();
+        const bool phased = cl.has_phase[k];
+#pragma unroll 1
+        for (int m = 0; m < 4; ++m) {
+          cx<R> bm[9], nn[9];
+          load9(bm, B + (j * 4 + m) * 9);
+          load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
+          if (phased) phase9(nn, cl.ph[k][m]);
+          wedge_acc(d, bm, nn);
+        }
+        const cx<R> s = dot9(a, d);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) cfma(u[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s);
+      }
     }
 #pragma unroll
     for (int w = 0; w < NW; ++w)
