@@ -42,10 +42,10 @@ N_TYPES = 6
 N_PROJ = 2
 UNITS_PER_SITE = N_TYPES * N_PROJ
 # Complex FMAs per site executed by the fused kernel (16 threads per site, one (i, l) pair
-# each): loop form 36 (wedge) + 2 x 9 (dots with Q_w); each of the two triangle passes
-# 4 x 36 (wedges a ^ B_m) + 4 m x 2 basis terms x 9 (dots) + 8 x 2 (projector coefficients);
-# Q set-up 18 x 3.  8 flops per complex FMA.
-FUSED_CFMA_PER_SITE = 16 * (36 + 18) + 2 * 16 * (4 * 36 + 8 * 9 + 8 * 2) + 18 * 3
+# each): two triangle passes of 4 wedges a ^ B_m (36 each), 4 m x 2 basis terms x 9 (dots)
+# and 2 x 2 (projector coefficients); the loop form's 2 x 9 dots with Q_w (its wedge is the
+# first pass's); Q set-up 18 x 3.  8 flops per complex FMA.
+FUSED_CFMA_PER_SITE = 16 * (2 * (4 * 36 + 8 * 9 + 2 * 2) + 2 * 9) + 18 * 3
 WORKLOAD = "baryon_2pt_24c64"
 METRIC = "GSite/s & HBM GB/s: mixed vs FP64 GPU contraction at <=1e-6 rel err/timeslice"
 

@@ -397,6 +397,79 @@ __device__ __forceinline__ void triangle_cliff_site(const BaryonSpin<R> &b, cons
     for (int w = 0; w < NW; ++w) vals[v * NW + w] = mul_phase(acc[v][w], p1);
 }
 
+// One triangle pass of the fused kernel (one (i, l) pair per thread) with the
+// gamma-basis projectors, on the shared-wedge order of triangle_cliff_site.
+// The m loop starts at m = l: with (A, B) = (P_i, P_j) its first wedge
+// A[i][perm2 l] ^ B[perm1 i][l] is the loop form's, so LOOP folds the two loop
+// types (dots with Q_w) into that iteration.  out[v*NW + w] = triangle values,
+// loop[v*NW + w] = loop values.
+template <class R, class S, int NW, bool LOOP>
+__device__ __forceinline__ void fused_triangle_pass(const BaryonSpin<R> &b, const S *A, const S *B, const S *N,
+                                                    const S *q, int i, int l, int c1sel, cx<R> *out, cx<R> *loop)
+{
+  const CliffordSet<R> &cl = b.cl;
+  const int j = b.perm1[i];
+  cx<R> a[9];
+  load9(a, A + (i * 4 + b.perm2[l]) * 9);
+  cx<R> u[NW];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) u[w] = czero<R>();
+  const bool two = cl.ng == 2;
+  cx<R> s0 = czero<R>(), s1 = czero<R>();  // per-term sums when there are two terms
+#pragma unroll 1
+  for (int mm = 0; mm < 4; ++mm) {
+    const int m = (l + mm) & 3;
+    cx<R> e[9];
+    {
+      cx<R> bm[9];
+      load9(bm, B + (j * 4 + m) * 9);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) e[k] = czero<R>();
+      wedge_acc(e, a, bm);
+    }
+    if constexpr (LOOP) {
+      if (mm == 0) {
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          cx<R> qw[9];
+          load9(qw, q + w * 9);
+          const cx<R> sq = dot9(e, qw);
+#pragma unroll
+          for (int v = 0; v < 2; ++v) loop[v * NW + w] = mul_phase(sq, (b.ph1[c1sel][i] + b.ph2[v][l]) & 3u);
+        }
+      }
+    }
+    if (two) {
+      cx<R> nn[9];
+      load9(nn, N + (cl.perm[0][m] * 4 + l) * 9);
+      s0 = cadd(s0, mul_phase(dot9(nn, e), cl.ph[0][m]));
+      load9(nn, N + (cl.perm[1][m] * 4 + l) * 9);
+      s1 = cadd(s1, mul_phase(dot9(nn, e), cl.ph[1][m]));
+    } else {
+#pragma unroll 1
+      for (int k = 0; k < cl.ng; ++k) {
+        cx<R> nn[9];
+        load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
+        const cx<R> s = mul_phase(dot9(nn, e), cl.ph[k][m]);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) cfma(u[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s);
+      }
+    }
+  }
+  if (two) {
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      cfma(u[w], cx<R> {cl.coef[w][0][0], cl.coef[w][0][1]}, s0);
+      cfma(u[w], cx<R> {cl.coef[w][1][0], cl.coef[w][1][1]}, s1);
+    }
+  }
+  const uint32_t p1 = b.ph1[c1sel][i];
+#pragma unroll
+  for (int w = 0; w < NW; ++w)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) out[v * NW + w] = mul_phase(u[w], (p1 + b.ph2[v][l]) & 3u);
+}
+
 // ------------------------------------------------------------------ ops --
 // Common compile-time configuration of an op: CW consumer warps (plus one
 // producer warp), TPS threads per site, NST ring stages.
@@ -459,24 +532,23 @@ template <class R, class S, int CW, int TPS, int NST, int NW>
 struct BaryonFusedCliffOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW);
   static constexpr bool FIELD = false;
+  static_assert(TPS == 16, "one (i, l) pair per thread");
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
     build_q_cliff<R, S, TPS, NW>(p.b, in[2], scratch, sub);
     __syncwarp();
-    cx<R> t[2 * NW];
-    loop_site<R, S, TPS, 2, NW>(p.b, in[0], in[1], scratch, sub, 0, t);  // IK_JL_NM, IL_JK_NM
+    const int i = sub >> 2, l = sub & 3;
+    cx<R> t[2 * NW], lp[2 * NW];
+    // IK_JM_NL, IL_JM_NK, with IK_JL_NM, IL_JK_NM folded into the first wedge
+    fused_triangle_pass<R, S, NW, true>(p.b, in[0], in[1], in[2], scratch, i, l, 0, t, lp);
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
-      vals[0 * NW + w] = t[0 * NW + w];
-      vals[2 * NW + w] = t[1 * NW + w];
-    }
-    triangle_cliff_site<R, S, TPS, 2, NW>(p.b, in[0], in[1], in[2], sub, 0, t);  // IK_JM_NL, IL_JM_NK
-#pragma unroll
-    for (int w = 0; w < NW; ++w) {
+      vals[0 * NW + w] = lp[0 * NW + w];
+      vals[2 * NW + w] = lp[1 * NW + w];
       vals[1 * NW + w] = t[0 * NW + w];
       vals[3 * NW + w] = t[1 * NW + w];
     }
-    triangle_cliff_site<R, S, TPS, 2, NW>(p.b, in[1], in[0], in[2], sub, 1, t);  // IM_JK_NL, IM_JL_NK
+    fused_triangle_pass<R, S, NW, false>(p.b, in[1], in[0], in[2], scratch, i, l, 1, t, lp);  // IM_JK_NL, IM_JL_NK
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
       vals[4 * NW + w] = t[0 * NW + w];
