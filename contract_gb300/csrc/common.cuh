@@ -163,6 +163,38 @@ template <class R, class S> __device__ __forceinline__ void load9(cx<R> out[9], 
   for (int k = 0; k < 9; ++k) out[k] = ld<R>(blk + k);
 }
 
+// A 9-complex colour block of a site slot whose spin-block index parity is
+// known at compile time.  Slots are 16-byte aligned and blocks are 72 bytes
+// apart, so an even block starts on a 16-byte boundary and an odd one 8 bytes
+// past it: complex64 blocks load as four 16-byte vectors plus one 8-byte
+// value (5 loads instead of 9).  Complex128 values are 16 bytes already.
+template <bool ODD, class R> __device__ __forceinline__ void load9p(cx<R> out[9], const float2 *blk)
+{
+  if constexpr (!ODD) {
+    const float4 *v = reinterpret_cast<const float4 *>(blk);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 t = v[q];
+      out[2 * q] = {R(t.x), R(t.y)};
+      out[2 * q + 1] = {R(t.z), R(t.w)};
+    }
+    out[8] = ld<R>(blk + 8);
+  } else {
+    out[0] = ld<R>(blk);
+    const float4 *v = reinterpret_cast<const float4 *>(blk + 1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 t = v[q];
+      out[1 + 2 * q] = {R(t.x), R(t.y)};
+      out[2 + 2 * q] = {R(t.z), R(t.w)};
+    }
+  }
+}
+template <bool ODD, class R> __device__ __forceinline__ void load9p(cx<R> out[9], const double2 *blk)
+{
+  load9(out, blk);
+}
+
 template <class R> __device__ __forceinline__ void phase9(cx<R> v[9], uint32_t p)
 {
 #pragma unroll

@@ -638,14 +638,17 @@ struct MesonAllSourceOp : OpBase<R, S, CW, 4, NST> {
     for (int g = 0; g < 16; ++g) vals[g] = czero<R>();
 #pragma unroll
     for (int l = 0; l < 4; ++l) {
-      cx<R> t[4];
+      cx<R> t[4], y[9];
+      if (l & 1) load9p<true>(y, in[1] + (j * 4 + l) * 9);  // block parity = parity of l
+      else load9p<false>(y, in[1] + (j * 4 + l) * 9);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
+        cx<R> x[9];
+        if (k & 1) load9p<true>(x, in[0] + (i * 4 + k) * 9);
+        else load9p<false>(x, in[0] + (i * 4 + k) * 9);
         t[k] = czero<R>();
-        const S *x = in[0] + (i * 4 + k) * 9;
-        const S *y = in[1] + (j * 4 + l) * 9;
 #pragma unroll
-        for (int e = 0; e < 9; ++e) cfma_conj(t[k], ld<R>(x + e), ld<R>(y + e));
+        for (int e = 0; e < 9; ++e) cfma_conj(t[k], x[e], y[e]);
       }
 #pragma unroll
       for (int g = 0; g < 16; ++g) vals[g] = cadd(vals[g], mul_phase(pick4(t, G.perm[g][l]), G.ph_g5g_t[g][l]));
@@ -916,17 +919,24 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
     constexpr GammaTables G = build_gamma_tables();
     const int s = sub >> 2, i = sub & 3, j = i ^ s;
     cx<R> T[4][4];
+    // Block (i, k) has the parity of k and block (j, l) that of l, so every
+    // colour block loads as 16-byte vectors.
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 4; ++k) {
+      cx<R> x[9];
+      if (k & 1) load9p<true>(x, in[0] + (i * 4 + k) * 9);
+      else load9p<false>(x, in[0] + (i * 4 + k) * 9);
 #pragma unroll
       for (int l = 0; l < 4; ++l) {
+        cx<R> y[9];
+        if (l & 1) load9p<true>(y, in[1] + (j * 4 + l) * 9);
+        else load9p<false>(y, in[1] + (j * 4 + l) * 9);
         cx<R> t = czero<R>();
-        const S *x = in[0] + (i * 4 + k) * 9;
-        const S *y = in[1] + (j * 4 + l) * 9;
 #pragma unroll
-        for (int e = 0; e < 9; ++e) cfma_conj(t, ld<R>(x + e), ld<R>(y + e));
+        for (int e = 0; e < 9; ++e) cfma_conj(t, x[e], y[e]);
         T[k][l] = t;
       }
+    }
     cx<R> V[16];
 #pragma unroll
     for (int b = 0; b < 16; ++b) {
