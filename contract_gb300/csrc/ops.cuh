@@ -868,6 +868,54 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
 //   V[b] = sum_l c_b(l) T[l ^ s_b][l]                    (all 16 Gamma_b)
 //   C[a][b] += c_a(i) V[b]   for the four Gamma_a of class s,
 // summed over the four threads i by a halving shuffle exchange.
+// The permutation of every Gamma(n) is r -> r ^ s for its class s, and
+// within a class the (g5 Gamma(a))^T row phases factor as
+//   ph(a, r) = beta_s(r) + alpha_a + 2 popcount(h_a & r)  (mod 4)
+// with h_a running over 0..3 (Walsh functions).  Hence the sum over spin
+// rows r of the four members of a class is one phase i^beta per row and a
+// four-point Walsh-Hadamard transform across the rows' threads, followed by
+// i^alpha per member.  ClassWalsh holds, per (class s, Walsh index h), the
+// member a and alpha, and beta per (s, r); built and checked at compile time.
+struct ClassWalsh {
+  uint32_t beta;     // 2 bits per (s, r), index 4 s + r
+  uint64_t member;   // 4 bits per (s, h), index 4 s + h
+  uint32_t alpha;    // 2 bits per (s, h)
+  bool ok;
+};
+CGB_HD constexpr ClassWalsh class_walsh()
+{
+  constexpr GammaTables G = build_gamma_tables();
+  ClassWalsh w {0u, 0ull, 0u, true};
+  for (int s = 0; s < 4; ++s) {
+    int base = -1, seen = 0;
+    for (int a = 0; a < 16; ++a) {
+      if (G.perm[a][0] != s) continue;
+      for (int r = 0; r < 4; ++r)
+        if (G.perm[a][r] != (r ^ s)) w.ok = false;
+      if (base < 0) {
+        base = a;
+        for (int r = 0; r < 4; ++r) w.beta |= (uint32_t)G.ph_g5g_t[a][r] << (2 * (4 * s + r));
+      }
+      int d[4] = {0, 0, 0, 0};
+      for (int r = 0; r < 4; ++r) d[r] = (G.ph_g5g_t[a][r] - G.ph_g5g_t[base][r] + 4) & 3;
+      const int alpha = d[0];
+      const int h0 = ((d[1] - alpha + 4) & 3) >> 1, h1 = ((d[2] - alpha + 4) & 3) >> 1;
+      for (int r = 0; r < 4; ++r) {
+        const int pc = ((r & 1) & h0) + (((r >> 1) & 1) & h1);
+        if (d[r] != ((alpha + 2 * pc) & 3)) w.ok = false;
+      }
+      const int h = h0 | (h1 << 1);
+      if (seen & (1 << h)) w.ok = false;
+      seen |= 1 << h;
+      w.member |= (uint64_t)a << (4 * (4 * s + h));
+      w.alpha |= (uint32_t)alpha << (2 * (4 * s + h));
+    }
+    if (seen != 15) w.ok = false;
+  }
+  return w;
+}
+static_assert(class_walsh().ok, "gamma classes must have the Walsh phase structure");
+
 template <class R, class S, int CW, int NST>
 struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 256;
@@ -889,34 +937,11 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
     return ((t * lz + z) * ly + y) * lx + x;
   }
 
-  // Gammas of each permutation class, four 4-bit indices packed per class.
-  __device__ static uint32_t class_members(int s)
-  {
-    constexpr GammaTables G = build_gamma_tables();
-    uint32_t packs[4] = {0, 0, 0, 0};
-    int fill[4] = {0, 0, 0, 0};
-    for (int n = 0; n < 16; ++n) {
-      const int c = G.perm[n][0];
-      packs[c] |= (uint32_t)n << (4 * fill[c]++);
-    }
-    return s == 0 ? packs[0] : (s == 1 ? packs[1] : (s == 2 ? packs[2] : packs[3]));
-  }
-
-  // (g5 Gamma_n)^T phase on spin row r, runtime n and r.
-  __device__ static uint32_t phase_g5g(int n, int r)
-  {
-    constexpr GammaTables G = build_gamma_tables();
-    uint32_t word[4] = {0, 0, 0, 0};  // 8 bits per gamma: four 2-bit row phases
-    for (int g = 0; g < 16; ++g)
-      for (int q = 0; q < 4; ++q) word[g >> 2] |= (uint32_t)G.ph_g5g_t[g][q] << (8 * (g & 3) + 2 * q);
-    const int wsel = n >> 2;
-    const uint32_t wv = wsel == 0 ? word[0] : (wsel == 1 ? word[1] : (wsel == 2 ? word[2] : word[3]));
-    return (wv >> (8 * (n & 3) + 2 * r)) & 3u;
-  }
 
   __device__ static void site(const OpParams<R> &, const S *const *in, S *, int sub, S *out)
   {
     constexpr GammaTables G = build_gamma_tables();
+    constexpr ClassWalsh CW8 = class_walsh();
     const int s = sub >> 2, i = sub & 3, j = i ^ s;
     cx<R> T[4][4];
     // Block (i, k) has the parity of k and block (j, l) that of l, so every
@@ -937,32 +962,49 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
         T[k][l] = t;
       }
     }
+    // V[b] = i^beta_s(i) sum_l (g5 Gamma(b))^T-phase(l) T[perm_b(l)][l]
+    const uint32_t beta = (CW8.beta >> (2 * (4 * s + i))) & 3u;
     cx<R> V[16];
 #pragma unroll
     for (int b = 0; b < 16; ++b) {
-      V[b] = czero<R>();
+      cx<R> v = czero<R>();
 #pragma unroll
-      for (int l = 0; l < 4; ++l) V[b] = cadd(V[b], mul_phase(T[G.perm[b][l]][l], G.ph_g5g_t[b][l]));
+      for (int l = 0; l < 4; ++l) v = cadd(v, mul_phase(T[G.perm[b][l]][l], G.ph_g5g_t[b][l]));
+      V[b] = mul_phase(v, beta);
     }
-    const uint32_t members = class_members(s);
-    const bool hi1 = i & 1, hi2 = i & 2;
-    const int b0 = (hi1 ? 8 : 0) + (hi2 ? 4 : 0);
+    // Walsh-Hadamard over the row bits of i (lanes ^1, ^2), reduce-scattering b:
+    // this thread ends with X[h][kk] for b = 8 i0 + 4 i1 + kk.
+    const uint32_t i0 = i & 1, i1 = (i >> 1) & 1;
+    cx<R> Y0[8], Y1[8];  // Walsh bit h0 = 0, 1 for b in [8 i0, 8 i0 + 8)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int a = (members >> (4 * q)) & 15;
-      const uint32_t pa = phase_g5g(a, i);
-      cx<R> X[8];
+    for (int k = 0; k < 8; ++k) {
+      const cx<R> own = i0 ? V[8 + k] : V[k], send = i0 ? V[k] : V[8 + k];
+      const cx<R> recv = shfl_xor(send, 1);
+      Y0[k] = cadd(own, recv);
+      const cx<R> d = {own.x - recv.x, own.y - recv.y};
+      Y1[k] = {flip_sign(d.x, i0), flip_sign(d.y, i0)};
+    }
+    cx<R> X[4][4];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const cx<R> w_lo = mul_phase(V[k], pa), w_hi = mul_phase(V[k + 8], pa);
-        const cx<R> keep = hi1 ? w_hi : w_lo, send = hi1 ? w_lo : w_hi;
-        X[k] = cadd(keep, shfl_xor(send, 1));
+    for (int kk = 0; kk < 4; ++kk) {
+#pragma unroll
+      for (int h0 = 0; h0 < 2; ++h0) {
+        const cx<R> *Y = h0 ? Y1 : Y0;
+        const cx<R> own = i1 ? Y[4 + kk] : Y[kk], send = i1 ? Y[kk] : Y[4 + kk];
+        const cx<R> recv = shfl_xor(send, 2);
+        X[h0][kk] = cadd(own, recv);
+        const cx<R> d = {own.x - recv.x, own.y - recv.y};
+        X[2 + h0][kk] = {flip_sign(d.x, i1), flip_sign(d.y, i1)};
       }
+    }
+    const int b0 = 8 * i0 + 4 * i1;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const cx<R> keep = hi2 ? X[k + 4] : X[k], send = hi2 ? X[k] : X[k + 4];
-        st(out + a * 16 + b0 + k, cadd(keep, shfl_xor(send, 2)));
-      }
+    for (int h = 0; h < 4; ++h) {
+      const int idx = 4 * s + h;
+      const int a = (int)((CW8.member >> (4 * idx)) & 15u);
+      const uint32_t alpha = (CW8.alpha >> (2 * idx)) & 3u;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) st(out + a * 16 + b0 + kk, mul_phase(X[h][kk], alpha));
     }
   }
 };
