@@ -195,6 +195,18 @@ template <bool ODD, class R> __device__ __forceinline__ void load9p(cx<R> out[9]
   load9(out, blk);
 }
 
+// Two consecutive complex values to a 16-byte (complex64) or 32-byte
+// (complex128) aligned address, as vector stores.
+__device__ __forceinline__ void st2(float2 *p, cx<float> a, cx<float> b)
+{
+  *reinterpret_cast<float4 *>(p) = make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void st2(double2 *p, cx<double> a, cx<double> b)
+{
+  p[0] = make_double2(a.x, a.y);
+  p[1] = make_double2(b.x, b.y);
+}
+
 template <class R> __device__ __forceinline__ void phase9(cx<R> v[9], uint32_t p)
 {
 #pragma unroll

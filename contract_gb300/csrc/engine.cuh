@@ -109,7 +109,8 @@ template <class Op> struct Smem {
   static constexpr size_t TAIL = EXTRA + (size_t)Op::EXTRA_BYTES * Op::SITES;
   static constexpr size_t tail_bytes()
   {
-    if constexpr (Op::FIELD) return 2ull * Op::SITES * OutLayout<Op>::SLOT;
+    if constexpr (Op::FIELD && Op::DIRECT_OUT) return 0;
+    else if constexpr (Op::FIELD) return 2ull * Op::SITES * OutLayout<Op>::SLOT;
     else return (size_t)Op::SITES * Op::NOUT * 2 * sizeof(typename Op::R);
   }
   static constexpr size_t BYTES = TAIL + tail_bytes();
@@ -373,6 +374,22 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
     const S *in[NIN];
 #pragma unroll
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
+    if constexpr (Op::DIRECT_OUT) {
+      // The op stores its outputs itself: pass this site's destination, or
+      // nullptr past the tile's end or for a destination outside the volume.
+      S *dst = nullptr;
+      if (site < n) {
+        const long long d = Op::out_index(ps, first + site);
+        if (d >= 0 && d < g.volume) dst = static_cast<S *>(p.out[0]) + d * Op::OUT_ELEMS;
+        else if (sub == 0) report(p.status, kDevErrBadWork, (unsigned int)(first + site));
+      }
+      Op::site(ps, in, scratch, sub, dst);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[stage]);
+      __syncwarp();
+      it.next(g);
+      continue;
+    }
     unsigned char *ob = outbuf + (size_t)(u & 1) * SPW * O::SLOT;
     Op::site(ps, in, scratch, sub, reinterpret_cast<S *>(ob + (size_t)local * O::SLOT));
     fence_proxy_async_smem();

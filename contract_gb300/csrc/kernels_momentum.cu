@@ -19,7 +19,7 @@
 namespace cgb {
 
 using MesonAllGammaP = MesonAllGammaOp<double, double2, 4, 3>;
-using MesonAllGammaM = MesonAllGammaOp<float, float2, 6, 2>;
+using MesonAllGammaM = MesonAllGammaOp<float, float2, 8, 2>;
 
 template <class R> __device__ __forceinline__ cx<R> pick(const cx<R> *g, int k)
 {

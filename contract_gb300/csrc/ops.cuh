@@ -480,6 +480,9 @@ template <class R_, class S_, int CW_, int TPS_, int NST_> struct OpBase {
   static constexpr int CW = CW_, TPS = TPS_, NST = NST_;
   static constexpr int SITES = CW_ * (32 / TPS_);
   static constexpr int THREADS = 32 * (CW_ + 1);
+  // Field ops: true when site() stores its outputs to global memory itself
+  // (the engine then passes the destination, or nullptr for a site to skip).
+  static constexpr bool DIRECT_OUT = false;
   static_assert(32 % TPS_ == 0, "a site's threads must sit in one warp");
 };
 
@@ -920,6 +923,8 @@ template <class R, class S, int CW, int NST>
 struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 256;
   static constexpr bool FIELD = true;
+  // Each thread's 16 outputs are four 32-byte runs: stored straight to HBM.
+  static constexpr bool DIRECT_OUT = true;
 
   __device__ static long long out_index(const OpParams<R> &p, long long site)
   {
@@ -998,13 +1003,15 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
       }
     }
     const int b0 = 8 * i0 + 4 * i1;
+    if (!out) return;  // a site past the end of the tile (the shuffles above still ran)
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
       const int idx = 4 * s + h;
       const int a = (int)((CW8.member >> (4 * idx)) & 15u);
       const uint32_t alpha = (CW8.alpha >> (2 * idx)) & 3u;
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) st(out + a * 16 + b0 + kk, mul_phase(X[h][kk], alpha));
+      S *dst = out + a * 16 + b0;  // 32-byte aligned
+      st2(dst, mul_phase(X[h][0], alpha), mul_phase(X[h][1], alpha));
+      st2(dst + 2, mul_phase(X[h][2], alpha), mul_phase(X[h][3], alpha));
     }
   }
 };
