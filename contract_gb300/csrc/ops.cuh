@@ -702,10 +702,12 @@ template <class R, class S, int CW, int TPS, int NST>
 struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 144;
   static constexpr bool FIELD = true;
+  static constexpr bool DIRECT_OUT = true;  // each thread's 72-byte blocks go straight to HBM
   __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)
   {
     const BaryonSpin<R> &b = p.b;
+    if (!out) return;  // a site past the end of the tile (no cross-thread work below)
     for (int blk = sub; blk < 16; blk += TPS) {
       const int m = blk / 4, l = blk % 4, k = b.perm2[l];
       cx<R> d[9];
@@ -747,6 +749,7 @@ template <class R, class S, int CW, int TPS, int NST, bool LOOP, int ROLE>
 struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = cbytes<S>(144) + 16, OUT_ELEMS = 144;
   static constexpr bool FIELD = true;
+  static constexpr bool DIRECT_OUT = true;  // each thread's 72-byte blocks go straight to HBM
   __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
 
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, S *out)
@@ -786,6 +789,7 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
       for (int blk = sub; blk < 16; blk += TPS) {
         const int n = blk / 4, m = blk % 4;
         const bool hit = pw.perm[m] == n;
+        if (!out) continue;  // a site past the end of the tile
 #pragma unroll
         for (int e = 0; e < 9; ++e) st(out + blk * 9 + e, hit ? mul_phase(r[e], pw.ph[m]) : czero<R>());
       }
@@ -797,6 +801,7 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
   __device__ static void field_blocks(const BaryonSpin<R> &b, const ProjOperand<R> &pw, const S *A, const S *B,
                                       const S *scratch, int sub, S *out)
   {
+    if (!out) return;  // a site past the end of the tile (no cross-thread work below)
     for (int blk = sub; blk < 16; blk += TPS) {
       cx<R> d[9];
 #pragma unroll
