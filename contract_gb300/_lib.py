@@ -56,6 +56,8 @@ SIGNATURES = {
                                c_int, c_int_p]),
     "contract_baryon_all_types": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, c_int,
                                          c_void_p, c_int, c_int_p]),
+    "contract_baryon_all_types_host": (None, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, c_int,
+                                         c_void_p, c_int, c_int_p]),
     "contract_baryon_all_types_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int,
                                                   c_int, c_void_p, c_int, c_int_p]),
     "contract_baryon_all_types_batch": (None, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),

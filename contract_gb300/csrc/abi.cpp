@@ -7,6 +7,7 @@
 // message and exits with -1, a failed CUDA call exits with its error code.
 // That stays the default; contract_set_error_mode(CONTRACT_ERRORS_RECORD)
 // (or CONTRACT_ERROR_MODE=record) records the error and skips the call instead.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -45,6 +46,12 @@ struct DevState {
   cgb::DeviceStatus *status = nullptr;
   void *ws = nullptr;
   size_t ws_bytes = 0;
+  // Host-input pipeline (contract_baryon_all_types_host): staging buffers,
+  // two copy streams and their events; created on first use.
+  void *pipe = nullptr;
+  size_t pipe_bytes = 0;
+  cudaStream_t copy[2] = {nullptr, nullptr};
+  cudaEvent_t copied[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr}, start = nullptr;
 };
 DevState g_dev[64];
 
@@ -639,6 +646,69 @@ bool make_mom_plan(cgb::MomPlan &plan, const int *lattice, const int *moms, int 
   return true;
 }
 
+// Arguments shared by the all-types entry points.
+bool all_types_args_ok(int gamma_ij, int gamma_kl, int nproj, const void *projectors, int precision)
+{
+  if (nproj < 1 || nproj > 2) return invalid("nproj must be 1 or 2 (got %d)", nproj);
+  if (!projectors) return invalid("projectors is NULL");
+  return gamma_ok(gamma_ij, "gamma_ij") && gamma_ok(gamma_kl, "gamma_kl") && prec_ok(precision);
+}
+
+// Inputs, outputs (nproj x 6 rows of `stride` values), spin tables and
+// projectors of the fused all-types op.
+void fill_all_types(OpParams<double> &p, const void *pi, const void *pj, const void *pn, void *correl, size_t stride,
+                    int gamma_ij, int gamma_kl, int nproj, const void *projectors)
+{
+  p.in[0] = pi;
+  p.in[1] = pj;
+  p.in[2] = pn;
+  for (int o = 0; o < 6 * nproj; ++o) p.out[o] = correl ? static_cast<char *>(correl) + o * stride * 16 : nullptr;
+  set_row(p.b.perm1, kG.perm[gamma_ij]);
+  set_row(p.b.perm2, kG.perm[gamma_kl]);
+  set_row(p.b.ph1[0], kG.ph[gamma_ij]);    // A = P_i groups
+  set_row(p.b.ph1[1], kG.ph_t[gamma_ij]);  // IM_* group (A = P_j)
+  set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);  // IK_JL_NM, IK_JM_NL, IM_JK_NL
+  set_row(p.b.ph2[1], kG.ph[gamma_kl]);    // IL_JK_NM, IL_JM_NK, IM_JL_NK
+  const double *pr = static_cast<const double *>(projectors);
+  const double *pw[2] = {pr, pr + 32};
+  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
+  fill_clifford(p.b.cl, pw, nproj, 0);
+}
+
+cudaError_t run_all_types(const cgb::Job &job, const OpParams<double> &p, int nproj)
+{
+  auto run = [&](const cgb::Job &j) { return cgb::launch_baryon_fused(j, nproj, p); };
+  return p.b.cl.ng <= nproj ? tuned_launch(cgb::Kind::BaryonFused, job, nproj, run) : run(job);
+}
+
+// Staging memory, copy streams and events of the host-input pipeline.
+bool pipeline_ready(DevState *s, size_t bytes)
+{
+  if (!s->copy[0]) {
+    for (int b = 0; b < 2; ++b) {
+      if (!cuda_ok(cudaStreamCreateWithFlags(&s->copy[b], cudaStreamNonBlocking), "cudaStreamCreateWithFlags") ||
+          !cuda_ok(cudaEventCreateWithFlags(&s->copied[b], cudaEventDisableTiming), "cudaEventCreateWithFlags") ||
+          !cuda_ok(cudaEventCreateWithFlags(&s->freed[b], cudaEventDisableTiming), "cudaEventCreateWithFlags"))
+        return false;
+    }
+    if (!cuda_ok(cudaEventCreateWithFlags(&s->start, cudaEventDisableTiming), "cudaEventCreateWithFlags")) return false;
+  }
+  if (bytes <= s->pipe_bytes) return true;
+  if (s->pipe) {
+    // Copies and kernels of an earlier call may still use the old buffer.
+    if (!cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize")) return false;
+    cudaFree(s->pipe);
+    s->pipe = nullptr;
+    s->pipe_bytes = 0;
+  }
+  if (cudaMalloc(&s->pipe, bytes) != cudaSuccess) {
+    s->pipe = nullptr;
+    return fail(CONTRACT_ERROR_OUT_OF_MEMORY, -1, "cannot allocate %zu bytes for the host-input pipeline", bytes);
+  }
+  s->pipe_bytes = bytes;
+  return true;
+}
+
 } // namespace
 
 // Only the C ABI is exported (the library is built with -fvisibility=hidden).
@@ -825,15 +895,7 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
                                size_t volume, int gamma_ij, int gamma_kl, int nproj, const void *projectors,
                                int precision, const int *lattice)
 {
-  if (nproj < 1 || nproj > 2) {
-    invalid("nproj must be 1 or 2 (got %d)", nproj);
-    return;
-  }
-  if (!projectors) {
-    invalid("projectors is NULL");
-    return;
-  }
-  if (!gamma_ok(gamma_ij, "gamma_ij") || !gamma_ok(gamma_kl, "gamma_kl") || !prec_ok(precision)) return;
+  if (!all_types_args_ok(gamma_ij, gamma_kl, nproj, projectors, precision)) return;
   if (!ptr_ok(correl, volume, "correl") || !ptr_ok(propag_i, volume, "propag_i") ||
       !ptr_ok(propag_j, volume, "propag_j") || !ptr_ok(propag_n, volume, "propag_n"))
     return;
@@ -843,24 +905,100 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
   DeviceWorkspace ws(s);
   job.ws = &ws;
   OpParams<double> p {};
-  p.in[0] = propag_i;
-  p.in[1] = propag_j;
-  p.in[2] = propag_n;
   const size_t stride = lattice ? (size_t)lattice[3] : volume;
-  for (int o = 0; o < 6 * nproj; ++o) p.out[o] = static_cast<char *>(correl) + o * stride * 16;
-  set_row(p.b.perm1, kG.perm[gamma_ij]);
-  set_row(p.b.perm2, kG.perm[gamma_kl]);
-  set_row(p.b.ph1[0], kG.ph[gamma_ij]);    // A = P_i groups
-  set_row(p.b.ph1[1], kG.ph_t[gamma_ij]);  // IM_* group (A = P_j)
-  set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);  // IK_JL_NM, IK_JM_NL, IM_JK_NL
-  set_row(p.b.ph2[1], kG.ph[gamma_kl]);    // IL_JK_NM, IL_JM_NK, IM_JL_NK
-  const double *pr = static_cast<const double *>(projectors);
-  const double *pw[2] = {pr, pr + 32};
-  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
-  fill_clifford(p.b.cl, pw, nproj, 0);
-  auto run = [&](const cgb::Job &j) { return cgb::launch_baryon_fused(j, nproj, p); };
-  const cudaError_t e = p.b.cl.ng <= nproj ? tuned_launch(cgb::Kind::BaryonFused, job, nproj, run) : run(job);
-  cuda_ok(e, "contract_baryon_all_types");
+  fill_all_types(p, propag_i, propag_j, propag_n, correl, stride, gamma_ij, gamma_kl, nproj, projectors);
+  cuda_ok(run_all_types(job, p, nproj), "contract_baryon_all_types");
+}
+
+void contract_baryon_all_types_host(void *correl, const void *propag_i, const void *propag_j, const void *propag_n,
+                                    size_t volume, int gamma_ij, int gamma_kl, int nproj, const void *projectors,
+                                    int precision, const int *lattice)
+{
+  if (!all_types_args_ok(gamma_ij, gamma_kl, nproj, projectors, precision)) return;
+  if (!lattice) {
+    invalid("contract_baryon_all_types_host needs the lattice");
+    return;
+  }
+  if (!correl || !propag_i || !propag_j || !propag_n) {
+    invalid("contract_baryon_all_types_host: NULL host pointer");
+    return;
+  }
+  cgb::Job full;
+  DevState *s = nullptr;
+  if (!make_job(full, precision, volume, lattice, &s)) return;
+  if (volume == 0) return;
+  const int lt = lattice[3];
+  const size_t half = (size_t)full.half_slice;  // sites per (parity, t)
+  const size_t site_in = 2304, site_c = precision == CONTRACT_C64 ? 1152 : 2304;
+  // Chunks of timeslices of about 256 MB of complex128 per propagator, and
+  // at least four chunks so that copies overlap the contractions.
+  size_t per_t = 2 * half * site_in;
+  int chunk = (int)std::max<size_t>(1, (256u << 20) / per_t);
+  chunk = std::min(chunk, std::max(1, (lt + 3) / 4));
+  chunk = std::min(chunk, lt);
+  const size_t chunk_sites = (size_t)chunk * 2 * half;
+  const size_t stage_bytes = ((chunk_sites * site_in + 255) / 256) * 256;
+  const size_t conv_bytes = precision == CONTRACT_C64 ? ((chunk_sites * site_c + 255) / 256) * 256 : 0;
+  const size_t out_bytes = ((size_t)6 * nproj * chunk * 16 + 255) / 256 * 256;
+  const size_t slot_bytes = 3 * stage_bytes + 3 * conv_bytes + out_bytes;
+  if (!pipeline_ready(s, 2 * slot_bytes)) return;
+
+  OpParams<double> p {};
+  fill_all_types(p, nullptr, nullptr, nullptr, nullptr, 0, gamma_ij, gamma_kl, nproj, projectors);
+  const void *host[3] = {propag_i, propag_j, propag_n};
+  DeviceWorkspace ws(s);
+  // Nothing of an earlier call may still read the staging buffers.
+  if (!cuda_ok(cudaEventRecord(s->start, g_stream), "cudaEventRecord")) return;
+  for (int b = 0; b < 2; ++b)
+    if (!cuda_ok(cudaStreamWaitEvent(s->copy[b], s->start, 0), "cudaStreamWaitEvent")) return;
+  const int nchunk = (lt + chunk - 1) / chunk;
+  for (int c = 0; c < nchunk; ++c) {
+    const int b = c & 1, t0 = c * chunk, nt = std::min(chunk, lt - t0);
+    char *slot = static_cast<char *>(s->pipe) + b * slot_bytes;
+    char *stage[3], *conv[3];
+    for (int q = 0; q < 3; ++q) {
+      stage[q] = slot + q * stage_bytes;
+      conv[q] = slot + 3 * stage_bytes + q * conv_bytes;
+    }
+    char *out = slot + 3 * stage_bytes + 3 * conv_bytes;
+    cudaStream_t cs = s->copy[b];
+    if (c >= 2 && !cuda_ok(cudaStreamWaitEvent(cs, s->freed[b], 0), "cudaStreamWaitEvent")) return;
+    // timeslices [t0, t0 + nt) of each parity, packed as a [2][nt][half] lattice
+    const size_t piece = (size_t)nt * half * site_in;
+    for (int q = 0; q < 3; ++q)
+      for (int par = 0; par < 2; ++par) {
+        const char *src = static_cast<const char *>(host[q]) + ((size_t)par * lt + t0) * half * site_in;
+        if (!cuda_ok(cudaMemcpyAsync(stage[q] + par * piece, src, piece, cudaMemcpyHostToDevice, cs),
+                     "cudaMemcpyAsync"))
+          return;
+      }
+    if (!cuda_ok(cudaEventRecord(s->copied[b], cs), "cudaEventRecord") ||
+        !cuda_ok(cudaStreamWaitEvent(g_stream, s->copied[b], 0), "cudaStreamWaitEvent"))
+      return;
+    const int clatt[4] = {lattice[0], lattice[1], lattice[2], nt};
+    cgb::Job job;
+    if (!make_job(job, precision, (size_t)nt * 2 * half, clatt)) return;
+    job.ws = &ws;
+    const char *in[3] = {stage[0], stage[1], stage[2]};
+    if (precision == CONTRACT_C64) {
+      for (int q = 0; q < 3; ++q) {
+        if (!cuda_ok(cgb::launch_convert(job, conv[q], stage[q], true), "contract_baryon_all_types_host")) return;
+        in[q] = conv[q];
+      }
+      if (!cuda_ok(cudaEventRecord(s->freed[b], g_stream), "cudaEventRecord")) return;
+    }
+    p.in[0] = in[0];
+    p.in[1] = in[1];
+    p.in[2] = in[2];
+    for (int o = 0; o < 6 * nproj; ++o) p.out[o] = out + (size_t)o * nt * 16;
+    if (!cuda_ok(run_all_types(job, p, nproj), "contract_baryon_all_types_host")) return;
+    if (precision != CONTRACT_C64 && !cuda_ok(cudaEventRecord(s->freed[b], g_stream), "cudaEventRecord")) return;
+    // out[o][t0 + t] for t < nt: rows of nt values into rows of Lt
+    if (!cuda_ok(cudaMemcpy2DAsync(static_cast<char *>(correl) + (size_t)t0 * 16, (size_t)lt * 16, out,
+                                   (size_t)nt * 16, (size_t)nt * 16, 6 * nproj, cudaMemcpyDeviceToHost, g_stream),
+                 "cudaMemcpy2DAsync"))
+      return;
+  }
 }
 
 int contract_baryon_all_types_noalloc(void *correl, const void *propag_i, const void *propag_j,

@@ -122,6 +122,18 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
                                size_t volume, int gamma_ij, int gamma_kl, int nproj, const void *projectors,
                                int precision, const int *lattice);
 
+/* contract_baryon_all_types from HOST complex128 propagators (pinned memory
+ * for full speed) into a HOST correl [6][nproj][Lt]; lattice required.
+ * Timeslice chunks of the three propagators are copied on two copy streams
+ * while earlier chunks are converted (CONTRACT_C64) and contracted on the
+ * library stream, so the copies overlap the work.  Asynchronous like every
+ * other call: synchronise the library stream before reading correl or
+ * changing the inputs.  Uses its own growable staging memory on the device.
+ * No counterpart in the reference. */
+void contract_baryon_all_types_host(void *correl, const void *propag_i, const void *propag_j, const void *propag_n,
+                                    size_t volume, int gamma_ij, int gamma_kl, int nproj, const void *projectors,
+                                    int precision, const int *lattice);
+
 /* contract_baryon_all_types with a non-NULL lattice, for callers that cannot
  * let the library allocate device memory (a pool allocator in the host
  * framework owns the free memory, cudaMalloc's implicit synchronisation is

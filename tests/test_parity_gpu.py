@@ -334,3 +334,32 @@ def test_sequential_sink_timeslice(api, props, c_oracle, c64):
         assert lib.contract_last_error() == 0, lib.contract_last_error_message()
         assert np.count_nonzero(got[tt != t_sink]) == 0
         assert rel_err(got, ref) < (1e-6 if c64 else TOL_C128), (ct, slot, t_sink)
+
+
+@pytest.mark.parametrize("c64", [False, True])
+@pytest.mark.parametrize("latt", [(4, 4, 4, 8), (6, 2, 2, 5)])
+def test_all_types_from_host_buffers(api, c64, latt):
+    """contract_baryon_all_types_host (timeslice chunks copied from pinned host
+    memory on two streams, contracted as they arrive) against the device call;
+    Lt = 5 leaves a short last chunk."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    pp = np.ascontiguousarray(api.projector_plus_minus())
+    ps = [eo.make_propagator(latt, 60 + s, 0.2 + 0.05 * s) for s in range(3)]
+    v = ps[0].shape[0]
+    lat = (ctypes.c_int * 4)(*latt)
+    prec = 1 if c64 else 0
+    dev = [cuda(x, c64) for x in ps]
+    ref = torch.empty((6, 2, latt[3]), dtype=torch.complex128, device="cuda")
+    lib.contract_baryon_all_types(ref.data_ptr(), *(x.data_ptr() for x in dev), v, 5, 5, 2, pp.ctypes.data, prec, lat)
+    host = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in ps]
+    out = torch.full((6, 2, latt[3]), float("nan"), dtype=torch.complex128).pin_memory()
+    for _ in range(2):  # the second call reuses the staging buffers and streams
+        lib.contract_baryon_all_types_host(out.data_ptr(), *(h.data_ptr() for h in host), v, 5, 5, 2,
+                                           pp.ctypes.data, prec, lat)
+    lib.contract_check_device()
+    torch.cuda.synchronize()
+    assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+    assert rel_err(out.numpy(), ref.cpu().numpy()) < (1e-6 if c64 else 1e-12)
