@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
       S *dst = nullptr;
       if (site < n) {
         const long long d = Op::out_index(ps, first + site);
-        if (d >= 0 && d < g.volume) dst = static_cast<S *>(p.out[0]) + d * Op::OUT_ELEMS;
+        if (d >= 0 && d < g.volume) dst = Op::out_ptr(ps, d, static_cast<S *>(p.out[0]));
         else if (sub == 0) report(p.status, kDevErrBadWork, (unsigned int)(first + site));
       }
       Op::site(ps, in, scratch, sub, dst);

@@ -20,6 +20,7 @@ namespace cgb {
 
 using MesonAllGammaP = MesonAllGammaOp<double, double2, 4, 3>;
 using MesonAllGammaM = MesonAllGammaOp<float, float2, 8, 2>;
+using MesonAllGammaSplitM = MesonAllGammaOp<float, float2, 8, 2, true>;  // field of the tensor-core path
 
 template <class R> __device__ __forceinline__ cx<R> pick(const cx<R> *g, int k)
 {
@@ -152,6 +153,7 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   for (int k = 0; k < 4; ++k) q.latt[k] = plan.latt[k];
   cudaError_t e;
   if (job.prec == Prec::C128) e = run_field<MesonAllGammaP>(job, q);
+  else if (tensor_cores) e = run_field<MesonAllGammaSplitM>(job, convert_params<float>(q));
   else e = run_field<MesonAllGammaM>(job, convert_params<float>(q));
   if (e != cudaSuccess) return e;
   if (tensor_cores)

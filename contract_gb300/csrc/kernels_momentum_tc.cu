@@ -17,19 +17,21 @@
 // dealt round-robin to persistent CTAs, so the CTAs running together share
 // the same phase tiles (L2-resident; the phase matrix does not depend on t).
 // Roles in a CTA (352 threads):
-//   warp 0     bulk copies of up to eight 1 KB rows of the complex64 per-site
-//              field per k-step into a 10-deep staging ring (HBM latency)
+//   warp 0     one bulk copy per k-step of the 8 sites x 128 pairs (8 KB) of
+//              the complex64 field, stored pair-half-major so that it is
+//              contiguous, into a 10-deep staging ring (HBM latency)
 //   warp 10    bulk copies of the 16 KB phase tile per k-step (both m-tiles,
 //              hi and lo, pre-tiled in global memory) into a 5-deep operand ring
-//   warp 1     allocates the 512 TMEM columns and issues the MMAs: for each
-//              of the two 128-row m-tiles three M=128, N=128, K=16 MMAs per
-//              k-step, into one of two accumulator buffers
+//   warp 1     allocates the 512 TMEM columns and issues the MMAs: three
+//              M=128 (pairs), N=256 (momentum rows), K=16 MMAs per k-step
+//              (field hi x phase hi, field hi x phase lo, field lo x phase hi)
+//              into one of two accumulator buffers of 256 columns
 //   warps 2-9  convert the staged FP32 values into the bf16 hi/lo field tile
 //              of the operand ring (four groups of two warps, each taking every
 //              fourth k-step), and all eight drain each accumulator buffer
 //              (kTcFlush k-steps of MMAs) into FP32 registers (tcgen05.ld) a
 //              few k-steps after its window ends, releasing it; at the end of
-//              a unit they store its 256 x 128 FP32 partial
+//              a unit they store its 128 x 256 FP32 partial
 // A final kernel sums the partials of each (t, p, n) in FP64 in a fixed order.
 // Every mbarrier wait is bounded; on a timeout the CTA stops, reports
 // kDevErrWaitTimeout, waits (bounded) for its copies and MMAs and frees TMEM.
@@ -50,18 +52,19 @@ constexpr int kTcGroups = 4;      // converter groups of two warps, one k-step e
 constexpr int kTcDrainLag = 3;    // k-steps converted past a window's end before draining it (< kTcOpStages)
 constexpr int kTcThreads = 352;   // 11 warps
 constexpr int kTcHeader = 1024;   // barriers, TMEM slot, abort flag
-constexpr int kTcABytes = 16384;  // 2 m-tiles x {hi, lo} x 128 x 16 bf16
-constexpr int kTcBBytes = 8192;   // {hi, lo} x 128 x 16 bf16
+constexpr int kTcABytes = 16384;  // phase tile: {hi, lo} x 256 rows x 16 bf16
+constexpr int kTcBBytes = 8192;   // field tile: {hi, lo} x 128 pairs x 16 bf16
 constexpr int kTcOpBytes = kTcABytes + kTcBBytes;
 constexpr int kTcStgBytes = 8192; // 8 sites x 128 pairs x complex64
 constexpr int kTcSmem = kTcHeader + kTcOpStages * kTcOpBytes + kTcStgStages * kTcStgBytes;
-constexpr uint32_t kTcIdesc = umma_idesc_bf16(128, 128);
-constexpr uint32_t kTcLbo = 16 * 128, kTcSbo = 128;  // 128-row tiles
+// D[pair][row] (+)= field[pair][k] * phase[row][k]: M = 128 pairs, N = 256 rows.
+constexpr uint32_t kTcIdesc = umma_idesc_bf16(128, 256);
+constexpr uint32_t kTcLbo128 = 16 * 128, kTcLbo256 = 32 * 128, kTcSbo = 128;
 
 struct TcParams {
-  const float2 *field;          // [Lt][V3][256] complex64, lexicographic sites
+  const float2 *field;          // [Lt][2 pair halves][V3][128] complex64, lexicographic sites
   const unsigned char *atiles;  // [MG][J][m-tile][hi, lo][4096 B]
-  float *partial;               // [U][m-tile][128 rows][128 pairs]
+  float *partial;               // [U][128 pairs][256 momentum rows]
   DeviceStatus *status;
   TcGeom g;
 };
@@ -172,14 +175,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
           break;
         }
         if (field) {
+          // the step's sites of this pair half are contiguous: [t][half][site][128 pairs]
           const long long s0 = (long long)j * 8;
           const int nvalid = (int)min(8LL, g.v3 - s0);
-          unsigned char *st = stgs + s * kTcStgBytes;
-          if (lane == 0) mbar_arrive_expect_tx(&full[s], (uint32_t)(nvalid * 1024));
-          __syncwarp();
-          if (lane < nvalid)
-            bulk_g2s(st + lane * 1024, p.field + (((size_t)w.t * g.v3 + s0 + lane) * 256 + w.h * 128), 1024,
-                     &full[s]);
+          if (lane == 0) {
+            mbar_arrive_expect_tx(&full[s], (uint32_t)(nvalid * 1024));
+            bulk_g2s(stgs + s * kTcStgBytes, p.field + (((size_t)w.t * 2 + w.h) * g.v3 + s0) * 128,
+                     (uint32_t)(nvalid * 1024), &full[s]);
+          }
         } else if (lane == 0) {
           mbar_arrive_expect_tx(&full[s], (uint32_t)kTcABytes);
           bulk_g2s(ops + s * kTcOpBytes, p.atiles + ((size_t)w.mg * g.j + j) * kTcABytes, kTcABytes, &full[s]);
@@ -216,17 +219,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
         tc_fence_after();
         if (lane == 0) {
           const uint32_t st = sbase + s * kTcOpBytes;
-          const uint64_t bh = umma_desc(st + kTcABytes, kTcLbo, kTcSbo);
-          const uint64_t bl = umma_desc(st + kTcABytes + 4096, kTcLbo, kTcSbo);
-#pragma unroll
-          for (int mt = 0; mt < 2; ++mt) {
-            const uint64_t ah = umma_desc(st + mt * 8192, kTcLbo, kTcSbo);
-            const uint64_t al = umma_desc(st + mt * 8192 + 4096, kTcLbo, kTcSbo);
-            const uint32_t d = tmem + buf * 256 + mt * 128;
-            umma_bf16(d, ah, bh, kTcIdesc, wf ? 0u : 1u);
-            umma_bf16(d, ah, bl, kTcIdesc, 1u);
-            umma_bf16(d, al, bh, kTcIdesc, 1u);
-          }
+          const uint64_t ph = umma_desc(st, kTcLbo256, kTcSbo);         // phase tile, hi
+          const uint64_t pl = umma_desc(st + 8192, kTcLbo256, kTcSbo);  // phase tile, lo
+          const uint64_t fh = umma_desc(st + kTcABytes, kTcLbo128, kTcSbo);
+          const uint64_t fl = umma_desc(st + kTcABytes + 4096, kTcLbo128, kTcSbo);
+          const uint32_t d = tmem + buf * 256;
+          umma_bf16(d, fh, ph, kTcIdesc, wf ? 0u : 1u);
+          umma_bf16(d, fh, pl, kTcIdesc, 1u);
+          umma_bf16(d, fl, ph, kTcIdesc, 1u);
           umma_commit(&op_empty[s]);
           if (wl) umma_commit(&acc_full[buf]);
         }
@@ -275,8 +275,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
       if (lane == 0) mbar_arrive(&acc_empty[b]);
       return true;
     };
-    auto store = [&](int unit) {
-      float4 *dst = reinterpret_cast<float4 *>(p.partial + (((size_t)unit * 2 + mt) * 128 + row) * 128);
+    auto store = [&](int unit) {  // this thread: pair `row`, momentum rows mt*128 .. mt*128 + 127
+      float4 *dst = reinterpret_cast<float4 *>(p.partial + ((size_t)unit * 128 + row) * 256 + mt * 128);
 #pragma unroll
       for (int k = 0; k < 32; ++k) {
         dst[k] = make_float4(run[4 * k], run[4 * k + 1], run[4 * k + 2], run[4 * k + 3]);
@@ -423,30 +423,30 @@ __global__ void __launch_bounds__(256) momentum_phase_tiles(unsigned char *__res
     w[s8 >> 2][0][s8 & 3] = bf16x2_bits(h);
     w[s8 >> 2][1][s8 & 3] = bf16x2_bits(l);
   }
-  unsigned char *tile = atiles + (((size_t)mg * nj + j) * 4 + mt * 2) * 4096;
+  // one 256-row tile per term (hi, lo): row mt * 128 + r
+  unsigned char *tile = atiles + ((size_t)mg * nj + j) * 16384;
+  const int row = mt * 128 + r;
 #pragma unroll
   for (int kc = 0; kc < 2; ++kc) {
-    const uint32_t off = (kc * 16 + (r >> 3)) * 128 + (r & 7) * 16;
+    const uint32_t off = (kc * 32 + (row >> 3)) * 128 + (row & 7) * 16;
     *reinterpret_cast<uint4 *>(tile + off) = make_uint4(w[kc][0][0], w[kc][0][1], w[kc][0][2], w[kc][0][3]);
-    *reinterpret_cast<uint4 *>(tile + 4096 + off) = make_uint4(w[kc][1][0], w[kc][1][1], w[kc][1][2], w[kc][1][3]);
+    *reinterpret_cast<uint4 *>(tile + 8192 + off) = make_uint4(w[kc][1][0], w[kc][1][1], w[kc][1][2], w[kc][1][3]);
   }
 }
 
 // out[p][t][n] = sum over the k-blocks of the unit partials, FP64, fixed order.
-__global__ void __launch_bounds__(256) momentum_tc_reduce(const float *__restrict__ partial, double2 *__restrict__ out,
+// One CTA per (pair-local n, half h, t + Lt * group); thread = momentum row.
+__global__ void __launch_bounds__(256) momentum_tc_reduce(const float *__restrict__ partial, double *__restrict__ out,
                                                           const __grid_constant__ TcGeom g, int np)
 {
-  const int pm = blockIdx.x, t = blockIdx.y, n = threadIdx.x;
-  if (pm >= np) return;
-  const int mg = pm >> 7, pr = pm & 127, mt = pr >> 6, pp = pr & 63, h = n >> 7, col = n & 127;
-  double re = 0.0, im = 0.0;
+  const int pl = blockIdx.x, h = blockIdx.y, t = blockIdx.z % g.lt, mg = blockIdx.z / g.lt, r = threadIdx.x;
+  const int pm = mg * 128 + (r >> 1);
+  double acc = 0.0;
   for (int jb = 0; jb < g.jb; ++jb) {
     const long long u = ((long long)(mg * g.jb + jb) * g.lt + t) * 2 + h;
-    const float *b = partial + ((size_t)u * 2 + mt) * 128 * 128;
-    re += (double)b[(2 * pp) * 128 + col];
-    im += (double)b[(2 * pp + 1) * 128 + col];
+    acc += (double)partial[((size_t)u * 128 + pl) * 256 + r];
   }
-  out[((size_t)pm * g.lt + t) * 256 + n] = make_double2(re, im);
+  if (pm < np) out[(((size_t)pm * g.lt + t) * 256 + h * 128 + pl) * 2 + (r & 1)] = acc;
 }
 
 } // namespace
@@ -492,7 +492,8 @@ cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom
   momentum_gemm_tc<<<grid, kTcThreads, kTcSmem, job.stream>>>(tp);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  momentum_tc_reduce<<<dim3(plan.np, g.lt), 256, 0, job.stream>>>(partial, static_cast<double2 *>(out), g, plan.np);
+  momentum_tc_reduce<<<dim3(128, 2, g.lt * g.mg), 256, 0, job.stream>>>(partial, static_cast<double *>(out), g,
+                                                                        plan.np);
   return cudaGetLastError();
 }
 

@@ -704,6 +704,7 @@ struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr bool FIELD = true;
   static constexpr bool DIRECT_OUT = true;  // each thread's 72-byte blocks go straight to HBM
   __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
+  __device__ static S *out_ptr(const OpParams<R> &, long long d, S *base) { return base + d * OUT_ELEMS; }
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)
   {
     const BaryonSpin<R> &b = p.b;
@@ -751,6 +752,7 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr bool FIELD = true;
   static constexpr bool DIRECT_OUT = true;  // each thread's 72-byte blocks go straight to HBM
   __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
+  __device__ static S *out_ptr(const OpParams<R> &, long long d, S *base) { return base + d * OUT_ELEMS; }
 
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, S *out)
   {
@@ -924,12 +926,32 @@ CGB_HD constexpr ClassWalsh class_walsh()
 }
 static_assert(class_walsh().ok, "gamma classes must have the Walsh phase structure");
 
-template <class R, class S, int CW, int NST>
+// SPLIT selects the layout [t][pair half][site][128 pairs] (pairs 0-127 and
+// 128-255 of a timeslice in separate planes) that the tensor-core projection
+// streams as contiguous 8-site tiles; otherwise [t][site][256 pairs].
+template <class R, class S, int CW, int NST, bool SPLIT = false>
 struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 256;
   static constexpr bool FIELD = true;
   // Each thread's 16 outputs are four 32-byte runs: stored straight to HBM.
   static constexpr bool DIRECT_OUT = true;
+
+  __device__ static long long sites_per_slice(const OpParams<R> &p)
+  {
+    return (long long)p.latt[0] * p.latt[1] * p.latt[2];
+  }
+  // Destination of site `d` (lexicographic index, 0 <= d < volume): the start
+  // of its 256 pairs, or with SPLIT of its first 128 (the second 128 follow
+  // one timeslice plane later).
+  __device__ static S *out_ptr(const OpParams<R> &p, long long d, S *base)
+  {
+    if constexpr (SPLIT) {
+      const long long v3 = sites_per_slice(p), t = d / v3;
+      return base + (d + t * v3) * 128;
+    } else {
+      return base + d * OUT_ELEMS;
+    }
+  }
 
   __device__ static long long out_index(const OpParams<R> &p, long long site)
   {
@@ -948,7 +970,7 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
   }
 
 
-  __device__ static void site(const OpParams<R> &, const S *const *in, S *, int sub, S *out)
+  __device__ static void site(const OpParams<R> &ps_, const S *const *in, S *, int sub, S *out)
   {
     constexpr GammaTables G = build_gamma_tables();
     constexpr ClassWalsh CW8 = class_walsh();
@@ -1014,7 +1036,9 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
       const int idx = 4 * s + h;
       const int a = (int)((CW8.member >> (4 * idx)) & 15u);
       const uint32_t alpha = (CW8.alpha >> (2 * idx)) & 3u;
-      S *dst = out + a * 16 + b0;  // 32-byte aligned
+      S *dst;  // 32-byte aligned
+      if constexpr (SPLIT) dst = out + (a >> 3) * sites_per_slice(ps_) * 128 + (a & 7) * 16 + b0;
+      else dst = out + a * 16 + b0;
       st2(dst, mul_phase(X[h][0], alpha), mul_phase(X[h][1], alpha));
       st2(dst + 2, mul_phase(X[h][2], alpha), mul_phase(X[h][3], alpha));
     }

@@ -363,3 +363,21 @@ def test_all_types_from_host_buffers(api, c64, latt):
     torch.cuda.synchronize()
     assert lib.contract_last_error() == 0, lib.contract_last_error_message()
     assert rel_err(out.numpy(), ref.cpu().numpy()) < (1e-6 if c64 else 1e-12)
+
+
+def test_pycontract_matrix_operands_as_in_reference_example(api, props):
+    """pycontract.baryonTwoPoint called as the reference's example does
+    (baryon_2pt.py:72-92): C g4 g5 and C g5 as 4x4 matrices (decomposed into a
+    basis index and a phase) and the projector (1 - g4)/2 (sent through the
+    general-projector path), against an einsum over the same matrices."""
+    from contract_gb300 import pycontract as pc
+    G = pc.gamma_matrices()
+    C = G[2] @ G[8]
+    cg_a, cg_b, proj = C @ G[8] @ G[15], C @ G[15], (G[0] - G[8]) / 2
+    pi, pj, pn = props
+    for t in (pc.BaryonContractType.IN_JK_ML, pc.BaryonContractType.IK_JL_MN):
+        got = pc.baryonTwoPoint(cuda(pi), cuda(pj), cuda(pn), t, cg_a, cg_b, proj).cpu().numpy()
+        si, sj, sn = eo._baryon_subscripts(int(t))
+        ref = np.einsum(f"abc,def,ij,kl,nm,x{si},x{sj},x{sn}->x", eo.EPS, eo.EPS, cg_a, cg_b, proj,
+                        eo._as_sites(pi), eo._as_sites(pj), eo._as_sites(pn), optimize=True)
+        assert rel_err(got, ref) < TOL_C128
