@@ -22,16 +22,12 @@ using MesonAllGammaP = MesonAllGammaOp<double, double2, 4, 3>;
 using MesonAllGammaM = MesonAllGammaOp<float, float2, 8, 2>;
 using MesonAllGammaSplitM = MesonAllGammaOp<float, float2, 8, 2, true>;  // field of the tensor-core path
 
-template <class R> __device__ __forceinline__ cx<R> pick(const cx<R> *g, int k)
-{
-  cx<R> r = g[0];
-#pragma unroll
-  for (int j = 1; j < kMomMaxPx; ++j)
-    if (k == j) r = g[j];
-  return r;
-}
-
 // One CTA per (z, t, chunk of (nx, ny) pairs); one thread per gamma pair.
+// Each thread's X-transform values G[nx] go through its own column of shared
+// memory, so the Y step reads G[q_ix[q]] with one load instead of selecting
+// among registers.
+template <class R> constexpr size_t plane_smem_bytes() { return (size_t)kMomMaxPx * 256 * 2 * sizeof(R); }
+
 template <class R, class S>
 __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, double2 *__restrict__ planes,
                                                     const __grid_constant__ MomPlan plan)
@@ -41,6 +37,10 @@ __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, dou
   const int nq = min(kMomQChunk, plan.nq - q0);
   __shared__ R phx[kMomMaxPx][kMomMaxL][2];
   __shared__ R phy[kMomQChunk][kMomMaxL][2];
+  extern __shared__ __align__(16) unsigned char plane_dyn[];
+  cx<R> *gxs = reinterpret_cast<cx<R> *>(plane_dyn);  // [kMomMaxPx][256]
+  __shared__ int qix[kMomQChunk];
+  if (g < kMomQChunk) qix[g] = g < nq ? plan.q_ix[q0 + g] : 0;
   for (int e = g; e < kMomMaxPx * kMomMaxL; e += blockDim.x) {
     const int ip = e / kMomMaxL, x = e % kMomMaxL;
     if (ip < plan.npx && x < lx) {
@@ -81,8 +81,11 @@ __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, dou
       }
     }
 #pragma unroll
+    for (int ip = 0; ip < kMomMaxPx; ++ip)
+      if (ip < plan.npx) gxs[ip * 256 + g] = gx[ip];
+#pragma unroll
     for (int q = 0; q < kMomQChunk; ++q)
-      if (q < nq) cfma(h[q], cx<R> {phy[q][y][0], phy[q][y][1]}, pick(gx, plan.q_ix[q0 + q]));
+      if (q < nq) cfma(h[q], cx<R> {phy[q][y][0], phy[q][y][1]}, gxs[qix[q] * 256 + g]);
   }
 #pragma unroll
   for (int q = 0; q < kMomQChunk; ++q)
@@ -161,10 +164,24 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
                               reinterpret_cast<float *>(ws + c_bytes + a_bytes), out);
 
   const dim3 grid(lz, lt, (plan.nq + kMomQChunk - 1) / kMomQChunk);
-  if (job.prec == Prec::C128)
-    plane_kernel<double, double2><<<grid, 256, 0, job.stream>>>(reinterpret_cast<const double2 *>(ws), planes, plan);
-  else
-    plane_kernel<float, float2><<<grid, 256, 0, job.stream>>>(reinterpret_cast<const float2 *>(ws), planes, plan);
+  if (job.prec == Prec::C128) {
+    // 32 KB of dynamic shared memory plus 34 KB static: above the default 48 KB
+    static bool attr[64] = {};
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 64 || !attr[dev]) {
+      e = cudaFuncSetAttribute(plane_kernel<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)plane_smem_bytes<double>());
+      if (e != cudaSuccess) return e;
+      if (dev < 64) attr[dev] = true;
+    }
+    plane_kernel<double, double2><<<grid, 256, plane_smem_bytes<double>(), job.stream>>>(
+      reinterpret_cast<const double2 *>(ws), planes, plan);
+  } else {
+    plane_kernel<float, float2><<<grid, 256, plane_smem_bytes<float>(), job.stream>>>(
+      reinterpret_cast<const float2 *>(ws), planes, plan);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   momentum_finalize<<<dim3(plan.nq, lt), 256, 0, job.stream>>>(planes, static_cast<double2 *>(out), plan);

@@ -392,6 +392,16 @@ __global__ void __launch_bounds__(256) momentum_phase_tiles(unsigned char *__res
   const int mt = threadIdx.x >> 7, r = threadIdx.x & 127;
   const int pm = mg * 128 + mt * 64 + (r >> 1), comp = r & 1;
   const int lx = plan.latt[0], ly = plan.latt[1], lz = plan.latt[2];
+  // The threads index the tables at different places: read them from shared
+  // memory, not from the (constant-bank) kernel parameters.
+  __shared__ double tab[6][kMomMaxL];
+  for (int e = threadIdx.x; e < 6 * kMomMaxL; e += blockDim.x) {
+    const int q = e / kMomMaxL, k = e % kMomMaxL;
+    const double *src = q == 0 ? plan.cosx : q == 1 ? plan.sinx : q == 2 ? plan.cosy : q == 3 ? plan.siny
+                        : q == 4 ? plan.cosz : plan.sinz;
+    tab[q][k] = src[k];
+  }
+  __syncthreads();
   const bool live = pm < plan.np;
   int nx = 0, ny = 0, nz = 0;
   if (live) {
@@ -401,20 +411,36 @@ __global__ void __launch_bounds__(256) momentum_phase_tiles(unsigned char *__res
     nz = plan.p_nz[pm];
   }
   uint32_t w[2][2][4];
+  // site coordinates and phase indices k = (n * x) mod L, advanced site by site
+  const long long s_first = (long long)j * 8;
+  int x = (int)(s_first % lx), y = (int)((s_first / lx) % ly), z = (int)(s_first / ((long long)lx * ly));
+  const int sx = ((nx % lx) + lx) % lx, sy = ((ny % ly) + ly) % ly;
+  int kx = (int)(((long long)sx * x) % lx), ky = (int)(((long long)sy * y) % ly);
 #pragma unroll
   for (int s8 = 0; s8 < 8; ++s8) {
-    const long long s = (long long)j * 8 + s8;
+    const long long s = s_first + s8;
     double re = 0.0, im = 0.0;
     if (live && s < v3) {
-      const int x = (int)(s % lx);
-      const long long r2 = s / lx;
-      const int y = (int)(r2 % ly), z = (int)(r2 / ly);
-      const int kx = ((nx * x) % lx + lx) % lx, ky = ((ny * y) % ly + ly) % ly, kz = ((nz * z) % lz + lz) % lz;
-      const double axr = plan.cosx[kx], axi = plan.sinx[kx], ayr = plan.cosy[ky], ayi = plan.siny[ky];
-      const double azr = plan.cosz[kz], azi = plan.sinz[kz];
+      const int kz = ((nz * z) % lz + lz) % lz;
+      const double axr = tab[0][kx], axi = tab[1][kx], ayr = tab[2][ky], ayi = tab[3][ky];
+      const double azr = tab[4][kz], azi = tab[5][kz];
       const double xyr = axr * ayr - axi * ayi, xyi = axr * ayi + axi * ayr;
       re = xyr * azr - xyi * azi;
       im = xyr * azi + xyi * azr;
+    }
+    // next site: x + 1, carrying into y and z
+    if (++x == lx) {
+      x = 0;
+      kx = 0;
+      if (++y == ly) {
+        y = 0;
+        ky = 0;
+        ++z;
+      } else if ((ky += sy) >= ly) {
+        ky -= ly;
+      }
+    } else if ((kx += sx) >= lx) {
+      kx -= lx;
     }
     const double a0 = comp ? im : re, a1 = comp ? re : -im;  // columns 2s (Re C) and 2s+1 (Im C)
     const __nv_bfloat162 h = __floats2bfloat162_rn((float)a0, (float)a1);

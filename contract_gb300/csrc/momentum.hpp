@@ -24,7 +24,7 @@ struct MomPlan {
 
 // Geometry of the tensor-core projection (kernels_momentum_tc.cu): k-steps of
 // 8 sites per timeslice, k-steps per work unit, units.
-constexpr int kTcUnitSteps = 256;
+constexpr int kTcUnitSteps = 512;
 struct TcGeom {
   long long v3;  // sites per timeslice
   int lt;        // timeslices
