@@ -499,7 +499,9 @@ void do_meson_all(void **correl, const void *pi, const void *pj, size_t volume, 
   set_row(p.m.ph1, kG.ph_g5g_t[gamma]);
   set_row(p.m.perm2, kG.perm[gamma]);
   set_row(p.m.ph2, kG.ph_g5g_t[gamma]);
-  cuda_ok(cgb::launch_meson_all(job, source, p), source ? "meson_all_source_two_point" : "meson_all_sink_two_point");
+  cuda_ok(tuned_launch(cgb::Kind::MesonAll, job, source ? 1 : 0,
+                       [&](const cgb::Job &j) { return cgb::launch_meson_all(j, source, p); }),
+          source ? "meson_all_source_two_point" : "meson_all_sink_two_point");
 }
 
 void do_baryon(void *correl, const void *pi, const void *pj, const void *pn, int type, size_t volume, int gij, int gkl,

@@ -45,6 +45,7 @@ __global__ void c64_to_c128(double2 *__restrict__ dst, const float2 *__restrict_
 }
 
 int meson_variants(Prec prec, const char *const **names);
+int meson_all_variants(Prec prec, bool source, const char *const **names);
 int baryon_variants(Prec prec, int form, const char *const **names);
 int fused_variants(Prec prec, int nw, const char *const **names);
 int field_variants(Prec prec, bool sequential, const char *const **names);
@@ -58,6 +59,7 @@ int launch_variants(Kind kind, Prec prec, int aux, const char *const **names)
   case Kind::BaryonFused: return fused_variants(prec, aux, names);
   case Kind::Diquark: return field_variants(prec, false, names);
   case Kind::Sequential: return field_variants(prec, true, names);
+  case Kind::MesonAll: return meson_all_variants(prec, aux != 0, names);
   }
   return 1;
 }

@@ -8,8 +8,6 @@ namespace cgb {
 using MesonP = MesonOp<double, double2, 2, 8, 3>;
 using MesonAllSrcP = MesonAllSourceOp<double, double2, 1, 3>;
 using MesonAllSnkP = MesonAllSinkOp<double, double2, 1, 3>;
-using MesonAllSrcM = MesonAllSourceOp<float, float2, 2, 4>;
-using MesonAllSnkM = MesonAllSinkOp<float, float2, 2, 4>;
 
 // complex64: HBM bound; the variants trade ring depth against CTAs per SM.
 static const VariantSet<float, 4> kMesonM = {
@@ -24,12 +22,32 @@ cudaError_t launch_meson(const Job &job, const OpParams<double> &p)
   return kMesonM.launch(job, convert_params<float>(p));
 }
 
+// complex64 all-source / all-sink: four threads (one spin row) per site, so a
+// consumer warp holds 8 sites (18.7 KB per ring stage).  Two CTAs of two
+// consumer warps with two stages, or one CTA of four or five.
+static const VariantSet<float, 4> kMesonAllSrcM = {
+  {run_scalar<MesonAllSourceOp<float, float2, 2, 2>>, run_scalar<MesonAllSourceOp<float, float2, 5, 2>>,
+   run_scalar<MesonAllSourceOp<float, float2, 4, 2>>, run_scalar<MesonAllSourceOp<float, float2, 2, 4>>},
+  {"cw2.tps4.st2", "cw5.tps4.st2", "cw4.tps4.st2", "cw2.tps4.st4"},
+  0};
+static const VariantSet<float, 4> kMesonAllSnkM = {
+  {run_scalar<MesonAllSinkOp<float, float2, 2, 2>>, run_scalar<MesonAllSinkOp<float, float2, 5, 2>>,
+   run_scalar<MesonAllSinkOp<float, float2, 4, 2>>, run_scalar<MesonAllSinkOp<float, float2, 2, 4>>},
+  {"cw2.tps4.st2", "cw5.tps4.st2", "cw4.tps4.st2", "cw2.tps4.st4"},
+  0};
+
 cudaError_t launch_meson_all(const Job &job, bool source, const OpParams<double> &p)
 {
   if (job.prec == Prec::C128)
     return source ? run_scalar<MesonAllSrcP>(job, p) : run_scalar<MesonAllSnkP>(job, p);
   const OpParams<float> q = convert_params<float>(p);
-  return source ? run_scalar<MesonAllSrcM>(job, q) : run_scalar<MesonAllSnkM>(job, q);
+  return source ? kMesonAllSrcM.launch(job, q) : kMesonAllSnkM.launch(job, q);
+}
+
+int meson_all_variants(Prec prec, bool source, const char *const **names)
+{
+  if (prec == Prec::C128) return 1;
+  return source ? kMesonAllSrcM.describe(names) : kMesonAllSnkM.describe(names);
 }
 
 int meson_variants(Prec prec, const char *const **names)
