@@ -702,7 +702,6 @@ template <class R, class S, int CW, int TPS, int NST>
 struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 144;
   static constexpr bool FIELD = true;
-  static constexpr bool DIRECT_OUT = true;  // each thread's 72-byte blocks go straight to HBM
   __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
   __device__ static S *out_ptr(const OpParams<R> &, long long d, S *base) { return base + d * OUT_ELEMS; }
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)
@@ -750,7 +749,6 @@ template <class R, class S, int CW, int TPS, int NST, bool LOOP, int ROLE>
 struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = cbytes<S>(144) + 16, OUT_ELEMS = 144;
   static constexpr bool FIELD = true;
-  static constexpr bool DIRECT_OUT = true;  // each thread's 72-byte blocks go straight to HBM
   __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
   __device__ static S *out_ptr(const OpParams<R> &, long long d, S *base) { return base + d * OUT_ELEMS; }
 
