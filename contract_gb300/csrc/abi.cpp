@@ -632,6 +632,33 @@ bool make_mom_plan(cgb::MomPlan &plan, const int *lattice, const int *moms, int 
     plan.p_q[p] = iq;
     plan.p_nz[p] = nz;
   }
+  // +nz / -nz groups of the Z transform (see MomPlan).  k = min(m, L - m) for m = nz mod L; the sign
+  // is + when m == k.  A momentum joins an open group of its k and sign slot,
+  // else starts one (duplicates get groups of their own).
+  auto key = [](int n, int L, bool &plus) {
+    const int m = ((n % L) + L) % L, k = m <= L - m ? m : L - m;
+    plus = m == k;
+    return k;
+  };
+  int ng = 0;
+  for (int q = 0; q < plan.nq; ++q) {
+    plan.q_g0[q] = ng;
+    for (int pm = 0; pm < nmom; ++pm) {
+      if (plan.p_q[pm] != q) continue;
+      bool plus;
+      const int k = key(plan.p_nz[pm], lattice[2], plus);
+      int gsel = -1;
+      for (int gi = plan.q_g0[q]; gi < ng && gsel < 0; ++gi)
+        if (plan.gz_k[gi] == k && (plus ? plan.gz_plus[gi] : plan.gz_minus[gi]) < 0) gsel = gi;
+      if (gsel < 0) {
+        gsel = ng++;
+        plan.gz_k[gsel] = k;
+        plan.gz_plus[gsel] = plan.gz_minus[gsel] = -1;
+      }
+      (plus ? plan.gz_plus[gsel] : plan.gz_minus[gsel]) = pm;
+    }
+  }
+  plan.q_g0[plan.nq] = ng;
   const double two_pi = 6.283185307179586476925286766559;
   for (int k = 0; k < lattice[0]; ++k) {
     plan.cosx[k] = std::cos(two_pi * k / lattice[0]);

@@ -94,44 +94,54 @@ __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, dou
 }
 
 // out[p][t][g] = sum_z exp(2 pi i nz z / Lz) planes[t][z][q(p)][g], FP64.
-// One CTA per ((nx, ny) pair q, t); each plane value is read once and feeds
-// every momentum of that pair (up to kMomMaxNzPerQ of them per pass).
-constexpr int kMomMaxNzPerQ = 16;
+// One CTA per ((nx, ny) pair q, t).  Each plane value is read once per pass
+// and feeds up to kMomGroupsPerPass Z groups of the pair; a group of +n and
+// -n accumulates C = sum cos * v and S = sum sin * v once for both momenta.
+constexpr int kMomGroupsPerPass = 8;
 __global__ void __launch_bounds__(256) momentum_finalize(const double2 *__restrict__ planes, double2 *__restrict__ out,
                                                           const __grid_constant__ MomPlan plan)
 {
   const int q = blockIdx.x, t = blockIdx.y, g = threadIdx.x;
-  const int lz = plan.latt[2];
-  __shared__ int plist[kMomMaxP];
-  __shared__ int nlist;
-  if (g == 0) {
-    int n = 0;
-    for (int p = 0; p < plan.np; ++p)
-      if (plan.p_q[p] == q) plist[n++] = p;
-    nlist = n;
+  const int lz = plan.latt[2], lt = plan.latt[3];
+  __shared__ double cz[kMomMaxL], sz[kMomMaxL];
+  for (int k = g; k < lz; k += blockDim.x) {
+    cz[k] = plan.cosz[k];
+    sz[k] = plan.sinz[k];
   }
   __syncthreads();
-  for (int base = 0; base < nlist; base += kMomMaxNzPerQ) {
-    const int cnt = min(kMomMaxNzPerQ, nlist - base);
-    double sx[kMomMaxNzPerQ], sy[kMomMaxNzPerQ];
+  const int g0 = plan.q_g0[q], g1 = plan.q_g0[q + 1];
+  for (int base = g0; base < g1; base += kMomGroupsPerPass) {
+    const int cnt = min(kMomGroupsPerPass, g1 - base);
+    double cx_[kMomGroupsPerPass], cy_[kMomGroupsPerPass], sx_[kMomGroupsPerPass], sy_[kMomGroupsPerPass];
+    int kk[kMomGroupsPerPass], step[kMomGroupsPerPass];
 #pragma unroll
-    for (int k = 0; k < kMomMaxNzPerQ; ++k) sx[k] = sy[k] = 0.0;
+    for (int k = 0; k < kMomGroupsPerPass; ++k) {
+      cx_[k] = cy_[k] = sx_[k] = sy_[k] = 0.0;
+      kk[k] = 0;
+      step[k] = k < cnt ? plan.gz_k[base + k] : 0;
+    }
     for (int z = 0; z < lz; ++z) {
       const double2 v = planes[((size_t)(t * lz + z) * plan.nq + q) * 256 + g];
 #pragma unroll
-      for (int k = 0; k < kMomMaxNzPerQ; ++k) {
+      for (int k = 0; k < kMomGroupsPerPass; ++k) {
         if (k < cnt) {
-          const int nz = plan.p_nz[plist[base + k]];
-          const int idx = ((nz * z) % lz + lz) % lz;
-          const double c = plan.cosz[idx], s = plan.sinz[idx];
-          sx[k] += c * v.x - s * v.y;
-          sy[k] += c * v.y + s * v.x;
+          const double c = cz[kk[k]], s = sz[kk[k]];
+          cx_[k] = fma(c, v.x, cx_[k]);
+          cy_[k] = fma(c, v.y, cy_[k]);
+          sx_[k] = fma(s, v.x, sx_[k]);
+          sy_[k] = fma(s, v.y, sy_[k]);
+          if ((kk[k] += step[k]) >= lz) kk[k] -= lz;  // k * z mod Lz
         }
       }
     }
 #pragma unroll
-    for (int k = 0; k < kMomMaxNzPerQ; ++k)
-      if (k < cnt) out[((size_t)plist[base + k] * plan.latt[3] + t) * 256 + g] = make_double2(sx[k], sy[k]);
+    for (int k = 0; k < kMomGroupsPerPass; ++k) {
+      if (k < cnt) {
+        const int pp = plan.gz_plus[base + k], pn = plan.gz_minus[base + k];
+        if (pp >= 0) out[((size_t)pp * lt + t) * 256 + g] = make_double2(cx_[k] - sy_[k], cy_[k] + sx_[k]);
+        if (pn >= 0) out[((size_t)pn * lt + t) * 256 + g] = make_double2(cx_[k] + sy_[k], cy_[k] - sx_[k]);
+      }
+    }
   }
 }
 
