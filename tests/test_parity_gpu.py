@@ -381,3 +381,35 @@ def test_pycontract_matrix_operands_as_in_reference_example(api, props):
         ref = np.einsum(f"abc,def,ij,kl,nm,x{si},x{sj},x{sn}->x", eo.EPS, eo.EPS, cg_a, cg_b, proj,
                         eo._as_sites(pi), eo._as_sites(pj), eo._as_sites(pn), optimize=True)
         assert rel_err(got, ref) < TOL_C128
+
+
+def test_momentum_grouping_edge_cases(api):
+    """Momentum lists that stress the +n / -n pairing of the Z transform:
+    duplicates, nz = +-Lz/2 (its own negative mod Lz), a lone -nz, and nx
+    beyond Lx/2; all three forms against the explicit phase sum."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    latt = (4, 4, 4, 2)
+    moms = np.array([[0, 0, 2], [0, 0, -2], [0, 0, 2], [1, 0, 0], [-1, 0, 0], [0, 0, 0], [0, 0, 0],
+                     [0, 1, -1], [3, 2, 1], [-3, 2, 5]], dtype=np.int32)
+    pi = eo.make_propagator(latt, 51, 0.2)
+    pj = eo.make_propagator(latt, 52, 0.3)
+    site = eo.meson_all_gamma(pi, pj).reshape(256, -1)
+    ref = eo.momentum_project(site, latt, moms).transpose(1, 2, 0)
+    sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real).T[None]
+    m = np.ascontiguousarray(moms)
+    for prec, tol in ((0, TOL_C128), (1, TOL_C64_TIMESLICE), (2, TOL_C64_TC)):
+        a, b = cuda(pi, prec >= 1), cuda(pj, prec >= 1)
+        out = torch.full((len(moms), latt[3], 256), float("nan"), dtype=torch.complex128, device="cuda")
+        lib.contract_meson_all_gamma_momentum(out.data_ptr(), a.data_ptr(), b.data_ptr(), pi.shape[0],
+                                              (ctypes.c_int * 4)(*latt),
+                                              m.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(moms), prec)
+        got = out.cpu().numpy()
+        assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+        if prec == 0:
+            assert rel_err(got, ref) < tol
+        else:
+            assert (np.abs(got - ref) / np.maximum(np.abs(ref), sig)).max() < tol
+    api.check_device()
