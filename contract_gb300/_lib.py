@@ -49,6 +49,7 @@ SIGNATURES = {
     "contract_workspace_bytes": (c_size_t, [c_int_p, c_int]),
     "contract_gamma_table": (None, [c_int_p, c_int_p]),
     "contract_convert_precision": (None, [c_void_p, c_void_p, c_size_t, c_int]),
+    "contract_convert_layout": (None, [c_void_p, c_void_p, c_int_p, c_int, c_int]),
     "contract_meson": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, c_int, c_int_p]),
     "contract_meson_all": (None, [ctypes.POINTER(c_void_p), c_void_p, c_void_p, c_size_t, c_int, c_int, c_int,
                                   c_int_p]),

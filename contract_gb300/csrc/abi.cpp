@@ -900,6 +900,28 @@ void contract_convert_precision(void *dst, const void *src, size_t volume, int t
   cuda_ok(cgb::launch_convert(job, dst, src, to_c64 != 0), "contract_convert_precision");
 }
 
+void contract_convert_layout(void *dst, const void *src, const int *lattice, int to_eo, int precision)
+{
+  if (!lattice) {
+    invalid("contract_convert_layout needs the lattice");
+    return;
+  }
+  if (!prec_ok(precision)) return;
+  const size_t volume = (size_t)std::max(0, lattice[0]) * std::max(0, lattice[1]) * std::max(0, lattice[2]) *
+                        std::max(0, lattice[3]);
+  if (!ptr_ok(dst, volume, "dst") || !ptr_ok(src, volume, "src")) return;
+  const size_t bytes = volume * 144 * (precision == CONTRACT_C64 ? 8 : 16);
+  const char *d = static_cast<const char *>(dst), *s = static_cast<const char *>(src);
+  if (volume && d < s + bytes && s < d + bytes) {
+    invalid("contract_convert_layout: dst and src overlap");
+    return;
+  }
+  cgb::Job job;
+  if (!make_job(job, precision, volume, lattice)) return;
+  cuda_ok(cgb::launch_layout(job, dst, src, lattice, to_eo != 0, precision == CONTRACT_C64 ? 1152 : 2304),
+          "contract_convert_layout");
+}
+
 void contract_meson(void *correl, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
                     int gamma_kl, int precision, const int *lattice)
 {

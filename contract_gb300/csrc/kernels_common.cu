@@ -64,6 +64,56 @@ int launch_variants(Kind kind, Prec prec, int aux, const char *const **names)
   return 1;
 }
 
+// Site reordering between lexicographic ((t*Lz + z)*Ly + y)*Lx + x and PyQUDA
+// even/odd ((par*Lt + t)*Lz + z)*Ly + y)*(Lx/2) + x/2, par = (x+y+z+t) & 1.
+// One thread per 16-byte piece of a site; a site's pieces are consecutive, so
+// reads and writes are contiguous runs of a whole site.
+__global__ void layout_kernel(uint4 *__restrict__ dst, const uint4 *__restrict__ src, long long volume,
+                              int pieces, int lx, int ly, int lz, int lt, int to_eo)
+{
+  const long long n = volume * pieces;
+  const int half = lx / 2;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const long long site = k / pieces;
+    const int w = (int)(k - site * pieces);
+    long long d;
+    if (to_eo) {
+      long long r = site;
+      const int x = (int)(r % lx);
+      r /= lx;
+      const int y = (int)(r % ly);
+      r /= ly;
+      const int z = (int)(r % lz);
+      const int t = (int)(r / lz);
+      const int par = (x + y + z + t) & 1;
+      d = ((((long long)par * lt + t) * lz + z) * ly + y) * half + x / 2;
+    } else {
+      long long r = site;
+      const int xh = (int)(r % half);
+      r /= half;
+      const int y = (int)(r % ly);
+      r /= ly;
+      const int z = (int)(r % lz);
+      r /= lz;
+      const int t = (int)(r % lt);
+      const int par = (int)(r / lt);
+      const int x = 2 * xh + ((par + t + z + y) & 1);
+      d = (((long long)t * lz + z) * ly + y) * lx + x;
+    }
+    dst[d * pieces + w] = src[k];
+  }
+}
+
+cudaError_t launch_layout(const Job &job, void *dst, const void *src, const int *latt, bool to_eo, int site_bytes)
+{
+  if (job.volume == 0) return cudaSuccess;
+  const int pieces = site_bytes / 16;
+  layout_kernel<<<job.num_sms * 8, 256, 0, job.stream>>>(static_cast<uint4 *>(dst), static_cast<const uint4 *>(src),
+                                                        job.volume, pieces, latt[0], latt[1], latt[2], latt[3],
+                                                        to_eo ? 1 : 0);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64)
 {
   const long long n = job.volume * 144;

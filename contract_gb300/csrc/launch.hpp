@@ -51,6 +51,8 @@ cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &
 cudaError_t launch_diquark(const Job &job, const OpParams<double> &p);
 cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParams<double> &p);
 cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64);
+// Propagator site order lexicographic <-> PyQUDA even/odd (site_bytes per site).
+cudaError_t launch_layout(const Job &job, void *dst, const void *src, const int *latt, bool to_eo, int site_bytes);
 // Address of this device's status word (a __device__ variable of the library).
 cudaError_t device_status_ptr(DeviceStatus **out);
 // Device address and size of the fixed scratch array used by the

@@ -97,6 +97,14 @@ void contract_gamma_table(int *perm, int *phase);
 /* complex128 <-> complex64 propagator copy of `volume` sites on the device. */
 void contract_convert_precision(void *dst, const void *src, size_t volume, int to_c64);
 
+/* Propagator site order on the device: to_eo != 0 reorders a lexicographic
+ * propagator (site ((t*Lz + z)*Ly + y)*Lx + x, e.g. QUDA's lexicographic or a
+ * gathered numpy field) into PyQUDA even/odd order [2][Lt][Lz][Ly][Lx/2]
+ * (parity (x+y+z+t) & 1); to_eo == 0 goes back.  Whole sites are moved
+ * (144 complex of `precision`); dst and src must not overlap.  No
+ * counterpart in the reference. */
+void contract_convert_layout(void *dst, const void *src, const int *lattice, int to_eo, int precision);
+
 /* ------------------------------------------------------ contractions --- */
 /* meson_two_point with a precision and optional per-timeslice output. */
 void contract_meson(void *correl, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,

@@ -413,3 +413,33 @@ def test_momentum_grouping_edge_cases(api):
         else:
             assert (np.abs(got - ref) / np.maximum(np.abs(ref), sig)).max() < tol
     api.check_device()
+
+
+@pytest.mark.parametrize("c64", [False, True])
+def test_layout_conversion_lexicographic_even_odd(api, c64):
+    """contract_convert_layout: lexicographic -> even/odd matches the
+    oracle's site coordinates exactly, and the round trip is the identity."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    latt = (6, 2, 4, 3)
+    lx, ly, lz, lt = latt
+    v = lx * ly * lz * lt
+    rng = np.random.default_rng(7)
+    lex = (rng.standard_normal((v, 144)) + 1j * rng.standard_normal((v, 144))).astype(np.complex128)
+    x, y, z, t = eo.eo_coords(latt)
+    want = lex[((t * lz + z) * ly + y) * lx + x]  # site e of the even/odd order
+    prec = 1 if c64 else 0
+    src = cuda(lex, c64)
+    dst = torch.full_like(src, float("nan"))
+    back = torch.full_like(src, float("nan"))
+    lat = (ctypes.c_int * 4)(*latt)
+    lib.contract_convert_layout(dst.data_ptr(), src.data_ptr(), lat, 1, prec)
+    lib.contract_convert_layout(back.data_ptr(), dst.data_ptr(), lat, 0, prec)
+    torch.cuda.synchronize()
+    assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+    ref = want.astype(np.complex64) if c64 else want
+    assert np.array_equal(dst.cpu().numpy(), ref)
+    assert torch.equal(back, src)
+
