@@ -470,6 +470,94 @@ __device__ __forceinline__ void fused_triangle_pass(const BaryonSpin<R> &b, cons
     for (int v = 0; v < 2; ++v) out[v * NW + w] = mul_phase(u[w], (p1 + b.ph2[v][l]) & 3u);
 }
 
+// Both triangle passes of the fused kernel in one m loop: with
+// a1 = P_i[i][perm2 l] and a2 = P_j[i][perm2 l], each N block n_km is loaded
+// once and dotted with both a1 ^ P_j[perm1 i][m] and a2 ^ P_i[perm1 i][m].
+// The loop form is folded into the m = l wedge of the first pass as in
+// fused_triangle_pass.  vals[type * NW + w], types in contract_enum.h order.
+template <class R, class S, int NW>
+__device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const S *Pi, const S *Pj, const S *N,
+                                                  const S *q, int i, int l, cx<R> *vals)
+{
+  const CliffordSet<R> &cl = b.cl;
+  const int j = b.perm1[i];
+  cx<R> a1[9], a2[9];
+  load9(a1, Pi + (i * 4 + b.perm2[l]) * 9);
+  load9(a2, Pj + (i * 4 + b.perm2[l]) * 9);
+  cx<R> u1[NW], u2[NW], lp[2 * NW];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) u1[w] = u2[w] = czero<R>();
+  const bool two = cl.ng == 2;
+  cx<R> s10 = czero<R>(), s11 = czero<R>(), s20 = czero<R>(), s21 = czero<R>();
+#pragma unroll 1
+  for (int mm = 0; mm < 4; ++mm) {
+    const int m = (l + mm) & 3;
+    cx<R> e1[9], e2[9];
+    {
+      cx<R> bm[9];
+      load9(bm, Pj + (j * 4 + m) * 9);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) e1[k] = czero<R>();
+      wedge_acc(e1, a1, bm);
+      load9(bm, Pi + (j * 4 + m) * 9);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) e2[k] = czero<R>();
+      wedge_acc(e2, a2, bm);
+    }
+    if (mm == 0) {
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        cx<R> qw[9];
+        load9(qw, q + w * 9);
+        const cx<R> sq = dot9(e1, qw);
+#pragma unroll
+        for (int v = 0; v < 2; ++v) lp[v * NW + w] = mul_phase(sq, (b.ph1[0][i] + b.ph2[v][l]) & 3u);
+      }
+    }
+    if (two) {
+      cx<R> nn[9];
+      load9(nn, N + (cl.perm[0][m] * 4 + l) * 9);
+      s10 = cadd(s10, mul_phase(dot9(nn, e1), cl.ph[0][m]));
+      s20 = cadd(s20, mul_phase(dot9(nn, e2), cl.ph[0][m]));
+      load9(nn, N + (cl.perm[1][m] * 4 + l) * 9);
+      s11 = cadd(s11, mul_phase(dot9(nn, e1), cl.ph[1][m]));
+      s21 = cadd(s21, mul_phase(dot9(nn, e2), cl.ph[1][m]));
+    } else {
+#pragma unroll 1
+      for (int k = 0; k < cl.ng; ++k) {
+        cx<R> nn[9];
+        load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
+        const cx<R> t1 = mul_phase(dot9(nn, e1), cl.ph[k][m]), t2 = mul_phase(dot9(nn, e2), cl.ph[k][m]);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          cfma(u1[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t1);
+          cfma(u2[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t2);
+        }
+      }
+    }
+  }
+  if (two) {
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      const cx<R> c0 {cl.coef[w][0][0], cl.coef[w][0][1]}, c1 {cl.coef[w][1][0], cl.coef[w][1][1]};
+      cfma(u1[w], c0, s10);
+      cfma(u1[w], c1, s11);
+      cfma(u2[w], c0, s20);
+      cfma(u2[w], c1, s21);
+    }
+  }
+  const uint32_t p1 = b.ph1[0][i], p2 = b.ph1[1][i];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    vals[0 * NW + w] = lp[0 * NW + w];                                 // IK_JL_NM
+    vals[2 * NW + w] = lp[1 * NW + w];                                 // IL_JK_NM
+    vals[1 * NW + w] = mul_phase(u1[w], (p1 + b.ph2[0][l]) & 3u);      // IK_JM_NL
+    vals[3 * NW + w] = mul_phase(u1[w], (p1 + b.ph2[1][l]) & 3u);      // IL_JM_NK
+    vals[4 * NW + w] = mul_phase(u2[w], (p2 + b.ph2[0][l]) & 3u);      // IM_JK_NL
+    vals[5 * NW + w] = mul_phase(u2[w], (p2 + b.ph2[1][l]) & 3u);      // IM_JL_NK
+  }
+}
+
 // ------------------------------------------------------------------ ops --
 // Common compile-time configuration of an op: CW consumer warps (plus one
 // producer warp), TPS threads per site, NST ring stages.
@@ -557,6 +645,21 @@ struct BaryonFusedCliffOp : OpBase<R, S, CW, TPS, NST> {
       vals[4 * NW + w] = t[0 * NW + w];
       vals[5 * NW + w] = t[1 * NW + w];
     }
+  }
+};
+
+// The same six types x NW projectors with both triangle passes in one m loop
+// (fused_merged_site): fewer N loads, more live registers.
+template <class R, class S, int CW, int TPS, int NST, int NW>
+struct BaryonFusedCliffMergedOp : OpBase<R, S, CW, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW);
+  static constexpr bool FIELD = false;
+  static_assert(TPS == 16, "one (i, l) pair per thread");
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    build_q_cliff<R, S, TPS, NW>(p.b, in[2], scratch, sub);
+    __syncwarp();
+    fused_merged_site<R, S, NW>(p.b, in[0], in[1], in[2], scratch, sub >> 2, sub & 3, vals);
   }
 };
 

@@ -69,13 +69,14 @@ def test_noalloc_matches_allocating_entry_point_twice(env, prec):
 
 
 def test_noalloc_rejects_lattices_beyond_the_static_scratch(env):
-    """2 x 1 x 1 x 8192: one site per half-timeslice, so 16384 partial records
-    of 7 warps x 12 outputs -- more than the 16 MiB array holds.  Real buffers
-    of the right size are passed; the call must refuse before any launch."""
+    """2 x 1 x 1 x 16384: one site per half-timeslice, so 32768 partial records
+    of (at least 3) consumer warps x 12 outputs x 16 bytes -- more than the
+    16 MiB array holds for every tile shape.  Real buffers of the right size are
+    passed; the call must refuse before any launch."""
     import torch
     lib, api, _ = env
-    latt = (2, 1, 1, 8192)
-    v = 2 * 8192
+    latt = (2, 1, 1, 16384)
+    v = 2 * 16384
     props = [torch.zeros((v, 4, 4, 3, 3), dtype=torch.complex64, device="cuda:0") for _ in range(3)]
     projs = np.ascontiguousarray(api.projector_plus_minus())
     out = torch.zeros((6, 2, latt[3]), dtype=torch.complex128, device="cuda:0")
