@@ -632,7 +632,7 @@ bool make_mom_plan(cgb::MomPlan &plan, const int *lattice, const int *moms, int 
     plan.p_q[p] = iq;
     plan.p_nz[p] = nz;
   }
-  // +nz / -nz groups of the Z transform (see MomPlan).  k = min(m, L - m) for m = nz mod L; the sign
+  // +n / -n groups of the X and Z transforms (see MomPlan).  k = min(m, L - m) for m = n mod L; the sign
   // is + when m == k.  A momentum joins an open group of its k and sign slot,
   // else starts one (duplicates get groups of their own).
   auto key = [](int n, int L, bool &plus) {
@@ -640,6 +640,20 @@ bool make_mom_plan(cgb::MomPlan &plan, const int *lattice, const int *moms, int 
     plus = m == k;
     return k;
   };
+  plan.ngx = 0;
+  for (int ip = 0; ip < plan.npx; ++ip) {
+    bool plus;
+    const int k = key(plan.px[ip], lattice[0], plus);
+    int gsel = -1;
+    for (int gi = 0; gi < plan.ngx && gsel < 0; ++gi)
+      if (plan.gx_k[gi] == k && (plus ? plan.gx_plus[gi] : plan.gx_minus[gi]) < 0) gsel = gi;
+    if (gsel < 0) {
+      gsel = plan.ngx++;
+      plan.gx_k[gsel] = k;
+      plan.gx_plus[gsel] = plan.gx_minus[gsel] = -1;
+    }
+    (plus ? plan.gx_plus[gsel] : plan.gx_minus[gsel]) = ip;
+  }
   int ng = 0;
   for (int q = 0; q < plan.nq; ++q) {
     plan.q_g0[q] = ng;

@@ -23,50 +23,52 @@ using MesonAllGammaM = MesonAllGammaOp<float, float2, 8, 2>;
 using MesonAllGammaSplitM = MesonAllGammaOp<float, float2, 8, 2, true>;  // field of the tensor-core path
 
 // One CTA per (z, t, chunk of (nx, ny) pairs); one thread per gamma pair.
-// Each thread's X-transform values G[nx] go through its own column of shared
-// memory, so the Y step reads G[q_ix[q]] with one load instead of selecting
-// among registers.
+// X transform: NG groups of +nx / -nx (C = sum cos * v, S = sum sin * v; the
+// group count is a template argument so that no predicated-off FMA is
+// issued).  Each thread's X values G[nx] go through its own column of shared
+// memory, so the Y step reads G[q_ix[q]] with one load; the Y step runs over
+// QC (>= the chunk's pair count) pairs.
 template <class R> constexpr size_t plane_smem_bytes() { return (size_t)kMomMaxPx * 256 * 2 * sizeof(R); }
 
-template <class R, class S>
+template <class R, class S, int NG, int QC>
 __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, double2 *__restrict__ planes,
                                                     const __grid_constant__ MomPlan plan)
 {
   const int z = blockIdx.x, t = blockIdx.y, q0 = blockIdx.z * kMomQChunk, g = threadIdx.x;
   const int lx = plan.latt[0], ly = plan.latt[1], lz = plan.latt[2];
   const int nq = min(kMomQChunk, plan.nq - q0);
-  __shared__ R phx[kMomMaxPx][kMomMaxL][2];
-  __shared__ R phy[kMomQChunk][kMomMaxL][2];
+  __shared__ R phx[NG][kMomMaxL][2];
+  __shared__ R phy[QC][kMomMaxL][2];
   extern __shared__ __align__(16) unsigned char plane_dyn[];
   cx<R> *gxs = reinterpret_cast<cx<R> *>(plane_dyn);  // [kMomMaxPx][256]
-  __shared__ int qix[kMomQChunk];
-  if (g < kMomQChunk) qix[g] = g < nq ? plan.q_ix[q0 + g] : 0;
-  for (int e = g; e < kMomMaxPx * kMomMaxL; e += blockDim.x) {
-    const int ip = e / kMomMaxL, x = e % kMomMaxL;
-    if (ip < plan.npx && x < lx) {
-      const int k = ((plan.px[ip] * x) % lx + lx) % lx;
-      phx[ip][x][0] = R(plan.cosx[k]);
-      phx[ip][x][1] = R(plan.sinx[k]);
+  __shared__ int qix[QC];
+  if (g < QC) qix[g] = g < nq ? plan.q_ix[q0 + g] : 0;
+  for (int e = g; e < NG * kMomMaxL; e += blockDim.x) {  // per X group: cos, sin of 2 pi k x / Lx
+    const int gi = e / kMomMaxL, x = e % kMomMaxL;
+    if (x < lx) {
+      const int k = (plan.gx_k[gi] * x) % lx;
+      phx[gi][x][0] = R(plan.cosx[k]);
+      phx[gi][x][1] = R(plan.sinx[k]);
     }
   }
-  for (int e = g; e < kMomQChunk * kMomMaxL; e += blockDim.x) {
+  for (int e = g; e < QC * kMomMaxL; e += blockDim.x) {
     const int q = e / kMomMaxL, y = e % kMomMaxL;
-    if (q < nq && y < ly) {
-      const int k = ((plan.q_ny[q0 + q] * y) % ly + ly) % ly;
-      phy[q][y][0] = R(plan.cosy[k]);
-      phy[q][y][1] = R(plan.siny[k]);
+    if (y < ly) {
+      const int k = q < nq ? ((plan.q_ny[q0 + q] * y) % ly + ly) % ly : 0;
+      phy[q][y][0] = q < nq ? R(plan.cosy[k]) : R(0);
+      phy[q][y][1] = q < nq ? R(plan.siny[k]) : R(0);
     }
   }
   __syncthreads();
-  cx<R> h[kMomQChunk];
+  cx<R> h[QC];
 #pragma unroll
-  for (int q = 0; q < kMomQChunk; ++q) h[q] = czero<R>();
+  for (int q = 0; q < QC; ++q) h[q] = czero<R>();
   const S *row = c + ((size_t)(t * lz + z) * ly * lx) * 256 + g;
   constexpr int XB = 8;  // loads in flight per thread
   for (int y = 0; y < ly; ++y) {
-    cx<R> gx[kMomMaxPx];
+    cx<R> gc[NG], gs[NG];
 #pragma unroll
-    for (int ip = 0; ip < kMomMaxPx; ++ip) gx[ip] = czero<R>();
+    for (int gi = 0; gi < NG; ++gi) gc[gi] = gs[gi] = czero<R>();
     const S *rowy = row + (size_t)y * lx * 256;
     for (int x0 = 0; x0 < lx; x0 += XB) {
       cx<R> v[XB];
@@ -76,21 +78,83 @@ __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, dou
       for (int u = 0; u < XB; ++u) {
         if (x0 + u >= lx) break;
 #pragma unroll
-        for (int ip = 0; ip < kMomMaxPx; ++ip)
-          if (ip < plan.npx) cfma(gx[ip], cx<R> {phx[ip][x0 + u][0], phx[ip][x0 + u][1]}, v[u]);
+        for (int gi = 0; gi < NG; ++gi) {
+          const R cs = phx[gi][x0 + u][0], sn = phx[gi][x0 + u][1];
+          gc[gi].x = fma(cs, v[u].x, gc[gi].x);
+          gc[gi].y = fma(cs, v[u].y, gc[gi].y);
+          gs[gi].x = fma(sn, v[u].x, gs[gi].x);
+          gs[gi].y = fma(sn, v[u].y, gs[gi].y);
+        }
       }
     }
+    // G(+k) = C + iS, G(-k) = C - iS
 #pragma unroll
-    for (int ip = 0; ip < kMomMaxPx; ++ip)
-      if (ip < plan.npx) gxs[ip * 256 + g] = gx[ip];
+    for (int gi = 0; gi < NG; ++gi) {
+      if (plan.gx_plus[gi] >= 0) gxs[plan.gx_plus[gi] * 256 + g] = {gc[gi].x - gs[gi].y, gc[gi].y + gs[gi].x};
+      if (plan.gx_minus[gi] >= 0) gxs[plan.gx_minus[gi] * 256 + g] = {gc[gi].x + gs[gi].y, gc[gi].y - gs[gi].x};
+    }
 #pragma unroll
-    for (int q = 0; q < kMomQChunk; ++q)
-      if (q < nq) cfma(h[q], cx<R> {phy[q][y][0], phy[q][y][1]}, gxs[qix[q] * 256 + g]);
+    for (int q = 0; q < QC; ++q) cfma(h[q], cx<R> {phy[q][y][0], phy[q][y][1]}, gxs[qix[q] * 256 + g]);
   }
 #pragma unroll
-  for (int q = 0; q < kMomQChunk; ++q)
+  for (int q = 0; q < QC; ++q)
     if (q < nq)
       planes[((size_t)(t * lz + z) * plan.nq + q0 + q) * 256 + g] = make_double2(double(h[q].x), double(h[q].y));
+}
+
+template <int NG> cudaError_t set_plane_smem_attr_ng()
+{
+  const int b = (int)plane_smem_bytes<double>();
+  cudaError_t e = cudaFuncSetAttribute(plane_kernel<double, double2, NG, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(plane_kernel<double, double2, NG, 9>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(plane_kernel<double, double2, NG, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(plane_kernel<double, double2, NG, kMomQChunk>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  return e;
+}
+
+inline cudaError_t set_plane_smem_attr()
+{
+  cudaError_t e = set_plane_smem_attr_ng<1>();
+  if (e == cudaSuccess) e = set_plane_smem_attr_ng<2>();
+  if (e == cudaSuccess) e = set_plane_smem_attr_ng<3>();
+  if (e == cudaSuccess) e = set_plane_smem_attr_ng<4>();
+  if (e == cudaSuccess) e = set_plane_smem_attr_ng<5>();
+  if (e == cudaSuccess) e = set_plane_smem_attr_ng<6>();
+  if (e == cudaSuccess) e = set_plane_smem_attr_ng<7>();
+  if (e == cudaSuccess) e = set_plane_smem_attr_ng<8>();
+  return e;
+}
+
+template <class R, class S, int NG>
+cudaError_t launch_plane_qc(const Job &job, const S *field, double2 *planes, const MomPlan &plan, dim3 grid)
+{
+  const int qc = plan.nq < kMomQChunk ? plan.nq : kMomQChunk;
+  const size_t smem = plane_smem_bytes<R>();
+  if (qc <= 4) plane_kernel<R, S, NG, 4><<<grid, 256, smem, job.stream>>>(field, planes, plan);
+  else if (qc <= 9) plane_kernel<R, S, NG, 9><<<grid, 256, smem, job.stream>>>(field, planes, plan);
+  else if (qc <= 16) plane_kernel<R, S, NG, 16><<<grid, 256, smem, job.stream>>>(field, planes, plan);
+  else plane_kernel<R, S, NG, kMomQChunk><<<grid, 256, smem, job.stream>>>(field, planes, plan);
+  return cudaGetLastError();
+}
+
+template <class R, class S>
+cudaError_t launch_plane(const Job &job, const S *field, double2 *planes, const MomPlan &plan, dim3 grid)
+{
+  switch (plan.ngx) {
+  case 1: return launch_plane_qc<R, S, 1>(job, field, planes, plan, grid);
+  case 2: return launch_plane_qc<R, S, 2>(job, field, planes, plan, grid);
+  case 3: return launch_plane_qc<R, S, 3>(job, field, planes, plan, grid);
+  case 4: return launch_plane_qc<R, S, 4>(job, field, planes, plan, grid);
+  case 5: return launch_plane_qc<R, S, 5>(job, field, planes, plan, grid);
+  case 6: return launch_plane_qc<R, S, 6>(job, field, planes, plan, grid);
+  case 7: return launch_plane_qc<R, S, 7>(job, field, planes, plan, grid);
+  case 8: return launch_plane_qc<R, S, 8>(job, field, planes, plan, grid);
+  default: return cudaErrorInvalidValue;
+  }
 }
 
 // out[p][t][g] = sum_z exp(2 pi i nz z / Lz) planes[t][z][q(p)][g], FP64.
@@ -175,24 +239,20 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
 
   const dim3 grid(lz, lt, (plan.nq + kMomQChunk - 1) / kMomQChunk);
   if (job.prec == Prec::C128) {
-    // 32 KB of dynamic shared memory plus 34 KB static: above the default 48 KB
+    // the complex128 form needs more than the default 48 KB of shared memory
     static bool attr[64] = {};
     int dev = 0;
     e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev >= 64 || !attr[dev]) {
-      e = cudaFuncSetAttribute(plane_kernel<double, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)plane_smem_bytes<double>());
+      e = set_plane_smem_attr();
       if (e != cudaSuccess) return e;
       if (dev < 64) attr[dev] = true;
     }
-    plane_kernel<double, double2><<<grid, 256, plane_smem_bytes<double>(), job.stream>>>(
-      reinterpret_cast<const double2 *>(ws), planes, plan);
+    e = launch_plane<double, double2>(job, reinterpret_cast<const double2 *>(ws), planes, plan, grid);
   } else {
-    plane_kernel<float, float2><<<grid, 256, plane_smem_bytes<float>(), job.stream>>>(
-      reinterpret_cast<const float2 *>(ws), planes, plan);
+    e = launch_plane<float, float2>(job, reinterpret_cast<const float2 *>(ws), planes, plan, grid);
   }
-  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   momentum_finalize<<<dim3(plan.nq, lt), 256, 0, job.stream>>>(planes, static_cast<double2 *>(out), plan);
   return cudaGetLastError();

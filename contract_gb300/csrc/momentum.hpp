@@ -20,9 +20,11 @@ struct MomPlan {
   double cosx[kMomMaxL], sinx[kMomMaxL];  // exp(2 pi i k / Lx)
   double cosy[kMomMaxL], siny[kMomMaxL];
   double cosz[kMomMaxL], sinz[kMomMaxL];
-  // The exp(+i theta) and exp(-i theta) Z transforms share C = sum cos(theta) v
-  // and S = sum sin(theta) v: nz -> C + iS, -nz -> C - iS.  Groups pair a
-  // momentum's nz (mod Lz) with -nz; an absent partner is -1.
+  // The exp(+i theta) and exp(-i theta) transforms share C = sum cos(theta) v
+  // and S = sum sin(theta) v: n -> C + iS, -n -> C - iS.  Groups pair a
+  // momentum component n (mod L) with -n; an absent partner is -1.
+  int ngx;                                                        // X groups
+  int gx_k[kMomMaxPx], gx_plus[kMomMaxPx], gx_minus[kMomMaxPx];  // k in [0, Lx/2]; px indices
   int q_g0[kMomMaxQ + 1];                                // Z groups of pair q: [q_g0[q], q_g0[q+1])
   int gz_k[kMomMaxP], gz_plus[kMomMaxP], gz_minus[kMomMaxP];     // k in [0, Lz/2]; momentum indices
 };
