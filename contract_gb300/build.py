@@ -31,6 +31,7 @@ SOURCES = [
     "kernels_field.cu",
     "kernels_momentum.cu",
     "kernels_momentum_tc.cu",
+    "kernels_momentum_fused.cu",
     "kernels_batch.cu",
     "noalloc.cu",
 ]

@@ -8,15 +8,24 @@
 //   1. MesonAllGammaOp (tile engine): C_ab(x) for all 256 pairs, written in
 //      lexicographic site order (HBM-bound: two propagators in, 256 complex out)
 //   2. plane_kernel: per (t, z) plane, X then Y transform of every C_ab into
-//      H[(nx, ny)][ab] (FP32 or FP64 arithmetic), stored in FP64
-//   3. momentum_finalize: Z transform and the sum over planes, in FP64.
+//      H[(nx, ny)][ab], in the form's arithmetic (FP64 planes for complex128,
+//      FP32 planes for the mixed form)
+//   3. momentum_finalize: Z transform and the sum over planes, returned in FP64.
+// The mixed form normally fuses 1 and 2 (kernels_momentum_fused.cu), so the
+// per-site values never reach HBM.
 // For 32^3 x 64 and 125 momenta that is ~25 GFLOP instead of 537 GFLOP.
 // Phase tables exp(2 pi i k / L) are computed in FP64 on the host from the
 // exact integer index k = (n * x) mod L.
+#include <algorithm>
+#include <cstdlib>
+
 #include "launch_variants.cuh"
 #include "momentum.hpp"
 
 namespace cgb {
+
+template <class R> struct Vec2 { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
 
 using MesonAllGammaP = MesonAllGammaOp<double, double2, 4, 3>;
 using MesonAllGammaM = MesonAllGammaOp<float, float2, 8, 2>;
@@ -31,7 +40,7 @@ using MesonAllGammaSplitM = MesonAllGammaOp<float, float2, 8, 2, true>;  // fiel
 template <class R> constexpr size_t plane_smem_bytes() { return (size_t)kMomMaxPx * 256 * 2 * sizeof(R); }
 
 template <class R, class S, int NG, int QC>
-__global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, double2 *__restrict__ planes,
+__global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, typename Vec2<R>::type *__restrict__ planes,
                                                     const __grid_constant__ MomPlan plan)
 {
   const int z = blockIdx.x, t = blockIdx.y, q0 = blockIdx.z * kMomQChunk, g = threadIdx.x;
@@ -99,7 +108,7 @@ __global__ void __launch_bounds__(256) plane_kernel(const S *__restrict__ c, dou
 #pragma unroll
   for (int q = 0; q < QC; ++q)
     if (q < nq)
-      planes[((size_t)(t * lz + z) * plan.nq + q0 + q) * 256 + g] = make_double2(double(h[q].x), double(h[q].y));
+      planes[((size_t)(t * lz + z) * plan.nq + q0 + q) * 256 + g] = {h[q].x, h[q].y};
 }
 
 template <int NG> cudaError_t set_plane_smem_attr_ng()
@@ -130,7 +139,8 @@ inline cudaError_t set_plane_smem_attr()
 }
 
 template <class R, class S, int NG>
-cudaError_t launch_plane_qc(const Job &job, const S *field, double2 *planes, const MomPlan &plan, dim3 grid)
+cudaError_t launch_plane_qc(const Job &job, const S *field, typename Vec2<R>::type *planes, const MomPlan &plan,
+                            dim3 grid)
 {
   const int qc = plan.nq < kMomQChunk ? plan.nq : kMomQChunk;
   const size_t smem = plane_smem_bytes<R>();
@@ -142,7 +152,8 @@ cudaError_t launch_plane_qc(const Job &job, const S *field, double2 *planes, con
 }
 
 template <class R, class S>
-cudaError_t launch_plane(const Job &job, const S *field, double2 *planes, const MomPlan &plan, dim3 grid)
+cudaError_t launch_plane(const Job &job, const S *field, typename Vec2<R>::type *planes, const MomPlan &plan,
+                         dim3 grid)
 {
   switch (plan.ngx) {
   case 1: return launch_plane_qc<R, S, 1>(job, field, planes, plan, grid);
@@ -157,56 +168,91 @@ cudaError_t launch_plane(const Job &job, const S *field, double2 *planes, const 
   }
 }
 
-// out[p][t][g] = sum_z exp(2 pi i nz z / Lz) planes[t][z][q(p)][g], FP64.
+// out[p][t][g] = sum_z exp(2 pi i nz z / Lz) planes[t][z][q(p)][g].
 // One CTA per ((nx, ny) pair q, t).  Each plane value is read once per pass
-// and feeds up to kMomGroupsPerPass Z groups of the pair; a group of +n and
-// -n accumulates C = sum cos * v and S = sum sin * v once for both momenta.
-constexpr int kMomGroupsPerPass = 8;
-__global__ void __launch_bounds__(256) momentum_finalize(const double2 *__restrict__ planes, double2 *__restrict__ out,
-                                                          const __grid_constant__ MomPlan plan)
+// and feeds up to CNT Z groups of the pair; a group of +n and -n accumulates
+// C = sum cos * v and S = sum sin * v once for both momenta.
+//   R = double (complex128 planes): FP64 phases and FMAs.
+//   R = float (complex64 planes, whose values are FP32 sums): FP32 phases and
+//     products, summed with a compensated (two-sum) accumulator and returned
+//     in FP64, so the sum over z adds no rounding beyond the products'.  The
+//     FP64 pipe (1/64 of the FP32 rate on this part) would otherwise bound
+//     the kernel.
+__device__ __forceinline__ void zacc(ChunkSum<double> &a, double c, double2 v)
+{
+  a.x = fma(c, v.x, a.x);
+  a.y = fma(c, v.y, a.y);
+}
+__device__ __forceinline__ void zacc(ChunkSum<float> &a, float c, float2 v) { a.add(cx<float> {c * v.x, c * v.y}); }
+
+template <class R, int CNT>
+__global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>::type *__restrict__ planes,
+                                                          double2 *__restrict__ out, const __grid_constant__ MomPlan plan)
 {
   const int q = blockIdx.x, t = blockIdx.y, g = threadIdx.x;
   const int lz = plan.latt[2], lt = plan.latt[3];
-  __shared__ double cz[kMomMaxL], sz[kMomMaxL];
+  __shared__ R cz[kMomMaxL], sz[kMomMaxL];
   for (int k = g; k < lz; k += blockDim.x) {
-    cz[k] = plan.cosz[k];
-    sz[k] = plan.sinz[k];
+    cz[k] = R(plan.cosz[k]);
+    sz[k] = R(plan.sinz[k]);
   }
   __syncthreads();
   const int g0 = plan.q_g0[q], g1 = plan.q_g0[q + 1];
-  for (int base = g0; base < g1; base += kMomGroupsPerPass) {
-    const int cnt = min(kMomGroupsPerPass, g1 - base);
-    double cx_[kMomGroupsPerPass], cy_[kMomGroupsPerPass], sx_[kMomGroupsPerPass], sy_[kMomGroupsPerPass];
-    int kk[kMomGroupsPerPass], step[kMomGroupsPerPass];
+  for (int base = g0; base < g1; base += CNT) {
+    const int cnt = min(CNT, g1 - base);
+    ChunkSum<R> ca[CNT], sa[CNT];
+    int kk[CNT], step[CNT];
 #pragma unroll
-    for (int k = 0; k < kMomGroupsPerPass; ++k) {
-      cx_[k] = cy_[k] = sx_[k] = sy_[k] = 0.0;
+    for (int k = 0; k < CNT; ++k) {
       kk[k] = 0;
       step[k] = k < cnt ? plan.gz_k[base + k] : 0;
     }
     for (int z = 0; z < lz; ++z) {
-      const double2 v = planes[((size_t)(t * lz + z) * plan.nq + q) * 256 + g];
+      const auto v = planes[((size_t)(t * lz + z) * plan.nq + q) * 256 + g];
 #pragma unroll
-      for (int k = 0; k < kMomGroupsPerPass; ++k) {
+      for (int k = 0; k < CNT; ++k) {
         if (k < cnt) {
-          const double c = cz[kk[k]], s = sz[kk[k]];
-          cx_[k] = fma(c, v.x, cx_[k]);
-          cy_[k] = fma(c, v.y, cy_[k]);
-          sx_[k] = fma(s, v.x, sx_[k]);
-          sy_[k] = fma(s, v.y, sy_[k]);
+          zacc(ca[k], cz[kk[k]], v);
+          zacc(sa[k], sz[kk[k]], v);
           if ((kk[k] += step[k]) >= lz) kk[k] -= lz;  // k * z mod Lz
         }
       }
     }
 #pragma unroll
-    for (int k = 0; k < kMomGroupsPerPass; ++k) {
+    for (int k = 0; k < CNT; ++k) {
       if (k < cnt) {
+        const double2 c = ca[k].value(), sn = sa[k].value();
         const int pp = plan.gz_plus[base + k], pn = plan.gz_minus[base + k];
-        if (pp >= 0) out[((size_t)pp * lt + t) * 256 + g] = make_double2(cx_[k] - sy_[k], cy_[k] + sx_[k]);
-        if (pn >= 0) out[((size_t)pn * lt + t) * 256 + g] = make_double2(cx_[k] + sy_[k], cy_[k] - sx_[k]);
+        if (pp >= 0) out[((size_t)pp * lt + t) * 256 + g] = make_double2(c.x - sn.y, c.y + sn.x);
+        if (pn >= 0) out[((size_t)pn * lt + t) * 256 + g] = make_double2(c.x + sn.y, c.y - sn.x);
       }
     }
   }
+}
+
+template <class R>
+cudaError_t launch_finalize(const Job &job, const typename Vec2<R>::type *planes, double2 *out, const MomPlan &plan)
+{
+  int most = 1;  // Z groups of the pair with the most
+  for (int q = 0; q < plan.nq; ++q) most = std::max(most, plan.q_g0[q + 1] - plan.q_g0[q]);
+  const dim3 grid(plan.nq, plan.latt[3]);
+  if (most <= 1) momentum_finalize<R, 1><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else if (most <= 2) momentum_finalize<R, 2><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else if (most <= 3) momentum_finalize<R, 3><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else if (most <= 4) momentum_finalize<R, 4><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else momentum_finalize<R, 8><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  return cudaGetLastError();
+}
+
+// CONTRACT_MOMENTUM_UNFUSED=1 selects the three-kernel mixed form (site
+// values through HBM), for comparison.
+static bool fused_disabled()
+{
+  static const bool off = [] {
+    const char *v = getenv("CONTRACT_MOMENTUM_UNFUSED");
+    return v && v[0] == '1';
+  }();
+  return off;
 }
 
 cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out,
@@ -214,16 +260,24 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
 {
   if (job.volume == 0) return cudaSuccess;
   if (tensor_cores && job.prec != Prec::C64) return cudaErrorInvalidValue;
+  const bool fused = !tensor_cores && job.prec == Prec::C64 && momentum_fused_supported(plan) && !fused_disabled();
   const size_t elem = job.prec == Prec::C128 ? sizeof(double2) : sizeof(float2);
-  const size_t c_bytes = ((size_t)job.volume * 256 * elem + 255) / 256 * 256;
+  const size_t c_bytes = fused ? 0 : ((size_t)job.volume * 256 * elem + 255) / 256 * 256;
   const int lz = plan.latt[2], lt = plan.latt[3];
   const TcGeom tg = make_tc_geom(plan);
   const size_t a_bytes = (tc_phase_bytes(tg) + 255) / 256 * 256;
   const size_t plane_bytes = tensor_cores ? a_bytes + tc_partial_bytes(tg)
-                                          : (size_t)lt * lz * plan.nq * 256 * sizeof(double2);
+                                          : (size_t)lt * lz * plan.nq * 256 * 2 * (job.prec == Prec::C128 ? 8 : 4);
   char *ws = static_cast<char *>(job.ws->get(c_bytes + plane_bytes));
   if (!ws) return cudaErrorMemoryAllocation;
-  double2 *planes = reinterpret_cast<double2 *>(ws + c_bytes);
+  double2 *planes = reinterpret_cast<double2 *>(ws + c_bytes);  // complex128 form
+  float2 *planes_m = reinterpret_cast<float2 *>(ws + c_bytes);   // mixed form
+
+  if (fused) {
+    cudaError_t e = launch_momentum_fused(job, p.in[0], p.in[1], planes_m, plan);
+    if (e != cudaSuccess) return e;
+    return launch_finalize<float>(job, planes_m, static_cast<double2 *>(out), plan);
+  }
 
   OpParams<double> q = p;
   q.out[0] = ws;
@@ -250,12 +304,12 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
       if (dev < 64) attr[dev] = true;
     }
     e = launch_plane<double, double2>(job, reinterpret_cast<const double2 *>(ws), planes, plan, grid);
-  } else {
-    e = launch_plane<float, float2>(job, reinterpret_cast<const float2 *>(ws), planes, plan, grid);
+    if (e != cudaSuccess) return e;
+    return launch_finalize<double>(job, planes, static_cast<double2 *>(out), plan);
   }
+  e = launch_plane<float, float2>(job, reinterpret_cast<const float2 *>(ws), planes_m, plan, grid);
   if (e != cudaSuccess) return e;
-  momentum_finalize<<<dim3(plan.nq, lt), 256, 0, job.stream>>>(planes, static_cast<double2 *>(out), plan);
-  return cudaGetLastError();
+  return launch_finalize<float>(job, planes_m, static_cast<double2 *>(out), plan);
 }
 
 } // namespace cgb

@@ -1,0 +1,296 @@
+// Fused all-gamma meson momentum projection, mixed form (complex64 storage,
+// FP32 arithmetic): the per-site 16 x 16 meson values and the X and Y
+// transforms of the separable projection in one kernel, so the 256 complex
+// values per site live only in shared memory.  The three-kernel form writes
+// them to HBM (2 KB per site) and reads them back; here HBM traffic is the
+// two propagators (2 x 1152 B per site) plus one FP64 plane per (t, z).
+//
+// One persistent CTA per SM walks (t, z) planes.  A plane's sites are taken
+// in row order -- for each y, both parities' half-rows -- in tiles of 16:
+//
+//   warps 0-7    site warps: each fetches its own two sites of a tile with
+//                cp.async.bulk into a per-warp kFNst-stage ring (its own full
+//                mbarriers, kFNst - 1 tiles ahead), runs MesonAllGammaOp on
+//                them and leaves the 256 values per site in one of two shared
+//                output buffers (ofull / oempty mbarriers)
+//   warps 8-15   transform warps: thread g owns gamma pair g; for each site of
+//                a row, C += cos(k x) v and S += sin(k x) v per X group; at
+//                the end of a row G(nx) -> shared column, then
+//                H[q] += exp(i ky y) G(nx(q)) for every (nx, ny) pair q
+//
+// Sixteen warps (no separate producer) leave 128 registers per thread.  At the
+// end of a plane each transform thread writes H[q] in FP64 to the plane
+// buffer; momentum_finalize applies the Z transform in FP64, as in the
+// three-kernel form.  Every mbarrier wait is bounded in wall time; a timed-out
+// wait reports kDevErrWaitTimeout, raises the CTA's abort flag and returns.
+#include "engine.cuh"
+#include "momentum.hpp"
+
+namespace cgb {
+
+namespace {
+
+using FusedSiteOp = MesonAllGammaOp<float, float2, 8, 2>;
+constexpr int kFCW = 8;                           // site warps (and transform warps)
+constexpr int kFSites = kFCW * 2;                 // sites per tile (16 threads per site)
+constexpr int kFNst = 3;                          // input ring stages
+constexpr int kFThreads = 32 * 2 * kFCW;          // 512
+using FL = SiteLayout<float2>;
+constexpr size_t kFStage = 2ull * kFSites * FL::SLOT;
+constexpr size_t kFOut = (size_t)kFSites * 256 * sizeof(float2);  // 32 KB per output buffer
+constexpr size_t kFStagesOff = 256;  // mbarriers: full[kFCW][kFNst], ofull[2], oempty[2]; abort flag at 248
+constexpr size_t kFOutOff = kFStagesOff + kFNst * kFStage;
+constexpr size_t kFGxOff = kFOutOff + 2 * kFOut;
+constexpr size_t kFSmem = kFGxOff + (size_t)kMomMaxPx * 256 * sizeof(float2);
+
+struct FusedArgs {
+  const char *in[2];  // complex64 propagators, PyQUDA even/odd order
+  float2 *planes;     // [Lt][Lz][nq][256], FP32 sums
+  DeviceStatus *status;
+  int tiles_per_plane;
+  OpParams<float> op;  // the site op's parameter block (unused by the non-split form)
+};
+
+static_assert(sizeof(FusedArgs) + sizeof(MomPlan) <= 32764, "kernel parameters exceed 32764 bytes");
+static_assert(kFSmem + sizeof(float) * 2 * kMomMaxL * (3 + kMomQChunk) + 4 * kMomQChunk <= 232448,
+              "fused momentum kernel does not fit in shared memory");
+
+// Site j (0 <= j < Lx Ly) of plane (t, z) in row order: y = j / Lx, then the
+// parity-0 half-row, then the parity-1 half-row.  Returns its even/odd index.
+__device__ __forceinline__ long long plane_site(const MomPlan &pl, int t, int z, int j)
+{
+  const int lx = pl.latt[0], ly = pl.latt[1], lz = pl.latt[2], lt = pl.latt[3], half = lx >> 1;
+  const int y = j / lx, r = j - y * lx, par = r >= half ? 1 : 0, xh = r - par * half;
+  return ((((long long)par * lt + t) * lz + z) * ly + y) * half + xh;
+}
+
+template <int NG, int QC>
+__global__ void __launch_bounds__(kFThreads, 1)
+  momentum_fused_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ MomPlan plan)
+{
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [kFCW][kFNst]
+  uint64_t *ofull = full + kFCW * kFNst;
+  uint64_t *oempty = ofull + 2;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 248);
+  float2 *obuf = reinterpret_cast<float2 *>(smem + kFOutOff);  // [2][kFSites][256]
+  __shared__ float phx[NG][kMomMaxL][2];
+  __shared__ float phy[QC][kMomMaxL][2];
+  __shared__ int qix[QC];
+
+  const int lx = plan.latt[0], ly = plan.latt[1], lz = plan.latt[2], lt = plan.latt[3];
+  const int units = lt * lz, tpp = a.tiles_per_plane, nsites = lx * ly;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kFCW * kFNst; ++s) mbar_init(&full[s], 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&ofull[b], kFCW);
+      mbar_init(&oempty[b], kFCW);
+    }
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int q = threadIdx.x; q < QC; q += blockDim.x) qix[q] = q < plan.nq ? plan.q_ix[q] : 0;
+  for (int e = threadIdx.x; e < NG * kMomMaxL; e += blockDim.x) {  // cos, sin of 2 pi k x / Lx per X group
+    const int gi = e / kMomMaxL, x = e % kMomMaxL;
+    const int k = x < lx ? (plan.gx_k[gi] * x) % lx : 0;
+    phx[gi][x][0] = float(plan.cosx[k]);
+    phx[gi][x][1] = float(plan.sinx[k]);
+  }
+  for (int e = threadIdx.x; e < QC * kMomMaxL; e += blockDim.x) {
+    const int q = e / kMomMaxL, y = e % kMomMaxL;
+    const bool on = q < plan.nq && y < ly;
+    const int k = on ? ((plan.q_ny[q] * y) % ly + ly) % ly : 0;
+    phy[q][y][0] = on ? float(plan.cosy[k]) : 0.f;
+    phy[q][y][1] = on ? float(plan.siny[k]) : 0.f;
+  }
+  __syncthreads();
+
+  // This CTA's tiles, numbered u = 0, 1, ...: tile k of its i-th plane
+  // (plane blockIdx.x + i * gridDim.x) is u = i * tpp + k.
+  const int my_units = blockIdx.x < units ? (units - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int ntiles = my_units * tpp;
+
+  if (warp < kFCW) {
+    // ---------------------------------------------------------- site warps
+    const int w = warp, local = lane >> 4, sub = lane & 15, site = w * 2 + local;
+    uint64_t *wfull = full + w * kFNst;
+    // Issue the copies of this warp's two sites of tile v into stage v % kFNst.
+    auto fetch = [&](int v) {
+      const int unit = blockIdx.x + (v / tpp) * gridDim.x, k = v % tpp;
+      const int t = unit / lz, z = unit - t * lz;
+      const int j0 = k * kFSites + w * 2, n = max(0, min(2, nsites - j0));
+      const int stage = v % kFNst;
+      if (lane == 0) mbar_arrive_expect_tx(&wfull[stage], (uint32_t)n * 2 * FL::SITE_BYTES);
+      __syncwarp();
+      if (lane < 2 * n) {
+        const int q = lane / n, s = lane - q * n;
+        bulk_g2s(smem + kFStagesOff + stage * kFStage + ((size_t)q * kFSites + w * 2 + s) * FL::SLOT,
+                 a.in[q] + plane_site(plan, t, z, j0 + s) * FL::SITE_BYTES, FL::SITE_BYTES, &wfull[stage]);
+      }
+    };
+    for (int v = 0; v < kFNst - 1 && v < ntiles; ++v) fetch(v);
+    for (int u = 0; u < ntiles; ++u) {
+      const int stage = u % kFNst, ob = u & 1;
+      if (u + kFNst - 1 < ntiles) {
+        // stage (u - 1) % kFNst: this warp finished reading it in tile u - 1
+        fence_proxy_async_smem();
+        __syncwarp();
+        fetch(u + kFNst - 1);
+      }
+      bool ok = mbar_wait_bounded(&wfull[stage], (u / kFNst) & 1, kWaitLimitNs);
+      if (ok && u >= 2) ok = mbar_wait_bounded(&oempty[ob], ((u >> 1) - 1) & 1, kWaitLimitNs);
+      if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
+        if (lane == 0) {
+          *abort_flag = 1;
+          report(a.status, kDevErrWaitTimeout, (unsigned int)u);
+          // copies this warp issued and has not waited for: tiles u .. u + kFNst - 1
+          for (int v = u; v < u + kFNst && v < ntiles; ++v)
+            mbar_wait_bounded(&wfull[v % kFNst], (v / kFNst) & 1, kWaitLimitNs / 8);
+        }
+        return;
+      }
+      const int n = min(kFSites, nsites - (u % tpp) * kFSites);
+      const unsigned char *sb = smem + kFStagesOff + stage * kFStage;
+      const float2 *in[2] = {reinterpret_cast<const float2 *>(sb + (size_t)site * FL::SLOT),
+                             reinterpret_cast<const float2 *>(sb + ((size_t)kFSites + site) * FL::SLOT)};
+      float2 *dst = site < n ? obuf + ((size_t)ob * kFSites + site) * 256 : nullptr;
+      FusedSiteOp::site(a.op, in, nullptr, sub, dst);
+      __threadfence_block();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&ofull[ob]);
+    }
+    return;
+  }
+
+  // ------------------------------------------------------ transform warps
+  const int g = threadIdx.x - 32 * kFCW;
+  const int half = lx >> 1;
+  const bool aligned = half % kFSites == 0;  // every tile lies in one half-row
+  cx<float> *gxs = reinterpret_cast<cx<float> *>(smem + kFGxOff);  // [kMomMaxPx][256], column g is this thread's
+  int u = 0;
+  for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+    const int t = unit / lz, z = unit - t * lz;
+    cx<float> h[QC];
+#pragma unroll
+    for (int q = 0; q < QC; ++q) h[q] = czero<float>();
+    cx<float> gc[NG], gs[NG];
+#pragma unroll
+    for (int gi = 0; gi < NG; ++gi) gc[gi] = gs[gi] = czero<float>();
+    int y = 0, r = 0;  // row and position in the row of the next site
+    auto xstep = [&](int gi, float cs, float sn, cx<float> v) {
+      gc[gi].x = fmaf(cs, v.x, gc[gi].x);
+      gc[gi].y = fmaf(cs, v.y, gc[gi].y);
+      gs[gi].x = fmaf(sn, v.x, gs[gi].x);
+      gs[gi].y = fmaf(sn, v.y, gs[gi].y);
+    };
+    // row y complete: G(+k) = C + iS, G(-k) = C - iS, then the Y step
+    auto end_row = [&]() {
+#pragma unroll
+      for (int gi = 0; gi < NG; ++gi) {
+        if (plan.gx_plus[gi] >= 0) gxs[plan.gx_plus[gi] * 256 + g] = {gc[gi].x - gs[gi].y, gc[gi].y + gs[gi].x};
+        if (plan.gx_minus[gi] >= 0) gxs[plan.gx_minus[gi] * 256 + g] = {gc[gi].x + gs[gi].y, gc[gi].y - gs[gi].x};
+        gc[gi] = gs[gi] = czero<float>();
+      }
+#pragma unroll
+      for (int q = 0; q < QC; ++q) cfma(h[q], cx<float> {phy[q][y][0], phy[q][y][1]}, gxs[qix[q] * 256 + g]);
+      ++y;
+    };
+    for (int k = 0; k < tpp; ++k, ++u) {
+      const int ob = u & 1;
+      const bool ok = mbar_wait_bounded(&ofull[ob], (u >> 1) & 1, kWaitLimitNs);
+      if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
+        if (lane == 0) {
+          *abort_flag = 1;
+          report(a.status, kDevErrWaitTimeout, (unsigned int)u);
+        }
+        return;
+      }
+      const cx<float> *col = reinterpret_cast<const cx<float> *>(obuf + (size_t)ob * kFSites * 256) + g;
+      if (aligned) {
+        // the tile is 16 sites of one half-row: x = x0, x0 + 2, ..., x0 + 30
+        const int r0 = (k * kFSites) % lx, par = r0 >= half ? 1 : 0;
+        const int x0 = 2 * (r0 - par * half) + ((par + t + z + y) & 1);
+#pragma unroll
+        for (int s = 0; s < kFSites; ++s) {
+          const cx<float> v = col[s * 256];
+#pragma unroll
+          for (int gi = 0; gi < NG; ++gi) xstep(gi, phx[gi][x0 + 2 * s][0], phx[gi][x0 + 2 * s][1], v);
+        }
+        if (r0 + kFSites == lx) end_row();
+      } else {
+        const int n = min(kFSites, nsites - k * kFSites);
+        for (int s = 0; s < n; ++s) {
+          const int par = r >= half ? 1 : 0;
+          const int x = 2 * (r - par * half) + ((par + t + z + y) & 1);
+          const cx<float> v = col[s * 256];
+#pragma unroll
+          for (int gi = 0; gi < NG; ++gi) xstep(gi, phx[gi][x][0], phx[gi][x][1], v);
+          if (++r == lx) {
+            end_row();
+            r = 0;
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&oempty[ob]);
+    }
+#pragma unroll
+    for (int q = 0; q < QC; ++q)
+      if (q < plan.nq)
+        a.planes[((size_t)unit * plan.nq + q) * 256 + g] = make_float2(h[q].x, h[q].y);
+  }
+}
+
+template <int NG, int QC> cudaError_t launch_fused_qc(const Job &job, const FusedArgs &a, const MomPlan &plan)
+{
+  static int bps_cache[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 64 || !bps_cache[dev]) {
+    e = cudaFuncSetAttribute(momentum_fused_kernel<NG, QC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFSmem);
+    if (e != cudaSuccess) return e;
+    if (dev < 64) bps_cache[dev] = 1;
+  }
+  const int units = plan.latt[3] * plan.latt[2];
+  const int grid = units < job.num_sms ? units : job.num_sms;
+  momentum_fused_kernel<NG, QC><<<grid, kFThreads, kFSmem, job.stream>>>(a, plan);
+  return cudaGetLastError();
+}
+
+template <int NG> cudaError_t launch_fused_ng(const Job &job, const FusedArgs &a, const MomPlan &plan)
+{
+  if (plan.nq <= 4) return launch_fused_qc<NG, 4>(job, a, plan);
+  if (plan.nq <= 9) return launch_fused_qc<NG, 9>(job, a, plan);
+  if (plan.nq <= 16) return launch_fused_qc<NG, 16>(job, a, plan);
+  return launch_fused_qc<NG, kMomQChunk>(job, a, plan);
+}
+
+} // namespace
+
+bool momentum_fused_supported(const MomPlan &plan)
+{
+  return plan.ngx >= 1 && plan.ngx <= 3 && plan.nq >= 1 && plan.nq <= kMomQChunk && plan.latt[0] >= 2 &&
+         plan.latt[0] % 2 == 0;
+}
+
+cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *in_j, float2 *planes,
+                                  const MomPlan &plan)
+{
+  if (!momentum_fused_supported(plan)) return cudaErrorInvalidValue;
+  FusedArgs a {};
+  a.in[0] = static_cast<const char *>(in_i);
+  a.in[1] = static_cast<const char *>(in_j);
+  a.planes = planes;
+  a.status = job.status;
+  a.tiles_per_plane = (plan.latt[0] * plan.latt[1] + kFSites - 1) / kFSites;
+  switch (plan.ngx) {
+  case 1: return launch_fused_ng<1>(job, a, plan);
+  case 2: return launch_fused_ng<2>(job, a, plan);
+  case 3: return launch_fused_ng<3>(job, a, plan);
+  default: return cudaErrorInvalidValue;
+  }
+}
+
+} // namespace cgb

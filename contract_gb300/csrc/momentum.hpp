@@ -47,6 +47,13 @@ size_t tc_partial_bytes(const TcGeom &g);
 cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom &g, const void *field,
                                unsigned char *atiles, float *partial, void *out);
 
+// Fused site + X/Y transform kernel of the mixed form (kernels_momentum_fused.cu):
+// writes the FP32 planes [Lt][Lz][nq][256] straight from the two complex64
+// propagators.  Supported for up to three X groups and kMomQChunk pairs.
+bool momentum_fused_supported(const MomPlan &plan);
+cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *in_j, float2 *planes,
+                                  const MomPlan &plan);
+
 // All-gamma meson correlators at the plan's momenta: out[p][t][16*16]
 // complex128 (device).  Uses job.ws for the per-site values and the plane
 // sums, or (tensor_cores, complex64 only) the phase tiles and unit partials

@@ -221,6 +221,33 @@ def test_meson_all_gamma_momentum(api, latt, c_oracle):
     api.check_device()
 
 
+@pytest.mark.parametrize("latt", [(6, 6, 2, 3), (10, 4, 2, 2), (4, 4, 16, 16)])
+def test_meson_momentum_fused_tiles(api, latt):
+    """The fused complex64 projection (site values and X/Y transforms in one
+    kernel): rows that cross 16-site tiles, a partial last tile per plane, and
+    more (t, z) planes than SMs, so that CTAs walk several planes."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    pi = eo.make_propagator(latt, 61, 0.2)
+    pj = eo.make_propagator(latt, 62, 0.25)
+    moms = eo.momentum_list(1)
+    site = eo.meson_all_gamma(pi, pj).reshape(256, -1)
+    ref = eo.momentum_project(site, latt, moms).transpose(1, 2, 0)
+    sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real).T[None]
+    m = np.ascontiguousarray(moms.astype(np.int32))
+    a, b = cuda(pi, True), cuda(pj, True)
+    out = torch.full((len(moms), latt[3], 256), float("nan"), dtype=torch.complex128, device="cuda")
+    lib.contract_meson_all_gamma_momentum(out.data_ptr(), a.data_ptr(), b.data_ptr(), pi.shape[0],
+                                          (ctypes.c_int * 4)(*latt),
+                                          m.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(moms), 1)
+    got = out.cpu().numpy()
+    assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+    assert (np.abs(got - ref) / np.maximum(np.abs(ref), sig)).max() < TOL_C64_TIMESLICE
+    api.check_device()
+
+
 def test_momentum_tensor_cores_two_momentum_groups(api):
     """CONTRACT_C64_TC with 147 momenta (two groups of 128 GEMM rows) on a
     lattice whose timeslice (6 x 6 x 4 = 144 sites) spans 18 k-steps."""
