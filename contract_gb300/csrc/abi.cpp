@@ -654,6 +654,12 @@ bool make_mom_plan(cgb::MomPlan &plan, const int *lattice, const int *moms, int 
     }
     (plus ? plan.gx_plus[gsel] : plan.gx_minus[gsel]) = ip;
   }
+  for (int gi = 1; gi < plan.ngx; ++gi)  // the nx = 0 group first: its transform is a plain sum
+    if (plan.gx_k[gi] == 0) {
+      std::swap(plan.gx_k[0], plan.gx_k[gi]);
+      std::swap(plan.gx_plus[0], plan.gx_plus[gi]);
+      std::swap(plan.gx_minus[0], plan.gx_minus[gi]);
+    }
   int ng = 0;
   for (int q = 0; q < plan.nq; ++q) {
     plan.q_g0[q] = ng;

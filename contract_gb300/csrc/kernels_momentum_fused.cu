@@ -30,7 +30,8 @@ namespace cgb {
 
 namespace {
 
-using FusedSiteOp = MesonAllGammaOp<float, float2, 8, 2>;
+// without the per-class phase, which the transform applies to its plane sums
+using FusedSiteOp = MesonAllGammaOp<float, float2, 8, 2, false, false>;
 constexpr int kFCW = 8;                           // site warps (and transform warps)
 constexpr int kFSites = kFCW * 2;                 // sites per tile (16 threads per site)
 constexpr int kFNst = 3;                          // input ring stages
@@ -167,6 +168,8 @@ __global__ void __launch_bounds__(kFThreads, 1)
   const int g = threadIdx.x - 32 * kFCW;
   const int half = lx >> 1;
   const bool aligned = half % kFSites == 0;  // every tile lies in one half-row
+  const uint32_t alpha = class_alpha(g >> 4);
+  const bool zero0 = plan.gx_k[0] == 0;      // X group 0 is nx = 0: C = sum v, S = 0
   cx<float> *gxs = reinterpret_cast<cx<float> *>(smem + kFGxOff);  // [kMomMaxPx][256], column g is this thread's
   int u = 0;
   for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
@@ -178,11 +181,12 @@ __global__ void __launch_bounds__(kFThreads, 1)
 #pragma unroll
     for (int gi = 0; gi < NG; ++gi) gc[gi] = gs[gi] = czero<float>();
     int y = 0, r = 0;  // row and position in the row of the next site
-    auto xstep = [&](int gi, float cs, float sn, cx<float> v) {
-      gc[gi].x = fmaf(cs, v.x, gc[gi].x);
-      gc[gi].y = fmaf(cs, v.y, gc[gi].y);
-      gs[gi].x = fmaf(sn, v.x, gs[gi].x);
-      gs[gi].y = fmaf(sn, v.y, gs[gi].y);
+    auto xstep = [&](int gi, float cs, float sn, cx<float> v) {  // packed FP32x2: (re, im) lanes
+      const float2 vv = make_float2(v.x, v.y);
+      const float2 c2 = __ffma2_rn(vv, make_float2(cs, cs), make_float2(gc[gi].x, gc[gi].y));
+      const float2 s2 = __ffma2_rn(vv, make_float2(sn, sn), make_float2(gs[gi].x, gs[gi].y));
+      gc[gi] = {c2.x, c2.y};
+      gs[gi] = {s2.x, s2.y};
     };
     // row y complete: G(+k) = C + iS, G(-k) = C - iS, then the Y step
     auto end_row = [&]() {
@@ -211,11 +215,22 @@ __global__ void __launch_bounds__(kFThreads, 1)
         // the tile is 16 sites of one half-row: x = x0, x0 + 2, ..., x0 + 30
         const int r0 = (k * kFSites) % lx, par = r0 >= half ? 1 : 0;
         const int x0 = 2 * (r0 - par * half) + ((par + t + z + y) & 1);
+        if (zero0) {
 #pragma unroll
-        for (int s = 0; s < kFSites; ++s) {
-          const cx<float> v = col[s * 256];
+          for (int s = 0; s < kFSites; ++s) {
+            const cx<float> v = col[s * 256];
+            gc[0].x += v.x;
+            gc[0].y += v.y;
 #pragma unroll
-          for (int gi = 0; gi < NG; ++gi) xstep(gi, phx[gi][x0 + 2 * s][0], phx[gi][x0 + 2 * s][1], v);
+            for (int gi = 1; gi < NG; ++gi) xstep(gi, phx[gi][x0 + 2 * s][0], phx[gi][x0 + 2 * s][1], v);
+          }
+        } else {
+#pragma unroll
+          for (int s = 0; s < kFSites; ++s) {
+            const cx<float> v = col[s * 256];
+#pragma unroll
+            for (int gi = 0; gi < NG; ++gi) xstep(gi, phx[gi][x0 + 2 * s][0], phx[gi][x0 + 2 * s][1], v);
+          }
         }
         if (r0 + kFSites == lx) end_row();
       } else {
@@ -237,8 +252,10 @@ __global__ void __launch_bounds__(kFThreads, 1)
     }
 #pragma unroll
     for (int q = 0; q < QC; ++q)
-      if (q < plan.nq)
-        a.planes[((size_t)unit * plan.nq + q) * 256 + g] = make_float2(h[q].x, h[q].y);
+      if (q < plan.nq) {
+        const cx<float> v = mul_phase(h[q], alpha);
+        a.planes[((size_t)unit * plan.nq + q) * 256 + g] = make_float2(v.x, v.y);
+      }
   }
 }
 

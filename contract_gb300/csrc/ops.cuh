@@ -987,6 +987,45 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
 // four-point Walsh-Hadamard transform across the rows' threads, followed by
 // i^alpha per member.  ClassWalsh holds, per (class s, Walsh index h), the
 // member a and alpha, and beta per (s, r); built and checked at compile time.
+// T[k][l] = sum_e x_k[e] conj(y_l[e]) for the four colour blocks x_k = xr[9k..]
+// and y_l = yr[9l..] of one spin row each, with packed FP32x2 FMAs (two lanes
+// of one instruction: (re, im) += (a.x, a.y) b.x and (a.y, -a.x) b.y), which
+// halves the issue slots of the products.  Colour index outermost, so only
+// one colour of each block is live; per element the FMA order is that of
+// cfma_conj, so the sums are the same to the bit.
+__device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[4][4], const float2 *xr, const float2 *yr)
+{
+  float2 acc[4][4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) acc[k][l] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    float2 a[4], ar[4], b[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      a[k] = xr[k * 9 + e];
+      ar[k] = make_float2(a[k].y, -a[k].x);
+    }
+#pragma unroll
+    for (int l = 0; l < 4; ++l) b[l] = yr[l * 9 + e];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      const float2 bx = make_float2(b[l].x, b[l].x), by = make_float2(b[l].y, b[l].y);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        acc[k][l] = __ffma2_rn(a[k], bx, acc[k][l]);
+        acc[k][l] = __ffma2_rn(ar[k], by, acc[k][l]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) T[k][l] = {acc[k][l].x, acc[k][l].y};
+}
+
 struct ClassWalsh {
   uint32_t beta;     // 2 bits per (s, r), index 4 s + r
   uint64_t member;   // 4 bits per (s, h), index 4 s + h
@@ -1027,10 +1066,23 @@ CGB_HD constexpr ClassWalsh class_walsh()
 }
 static_assert(class_walsh().ok, "gamma classes must have the Walsh phase structure");
 
+// The phase i^alpha that MesonAllGammaOp applies to every output of first
+// gamma index a.
+CGB_HD constexpr uint32_t class_alpha(int a)
+{
+  constexpr ClassWalsh W = class_walsh();
+  uint32_t al = 0;
+  for (int idx = 0; idx < 16; ++idx)
+    if ((int)((W.member >> (4 * idx)) & 15u) == a) al = (W.alpha >> (2 * idx)) & 3u;
+  return al;
+}
+
 // SPLIT selects the layout [t][pair half][site][128 pairs] (pairs 0-127 and
 // 128-255 of a timeslice in separate planes) that the tensor-core projection
 // streams as contiguous 8-site tiles; otherwise [t][site][256 pairs].
-template <class R, class S, int CW, int NST, bool SPLIT = false>
+// ALPHA = false leaves out the constant phase i^alpha of each first-gamma
+// index a (class_alpha(a)); a linear consumer applies it once to its sums.
+template <class R, class S, int CW, int NST, bool SPLIT = false, bool ALPHA = true>
 struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 256;
   static constexpr bool FIELD = true;
@@ -1077,22 +1129,26 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
     constexpr ClassWalsh CW8 = class_walsh();
     const int s = sub >> 2, i = sub & 3, j = i ^ s;
     cx<R> T[4][4];
-    // Block (i, k) has the parity of k and block (j, l) that of l, so every
-    // colour block loads as 16-byte vectors.
+    if constexpr (sizeof(R) == 4) {
+      conj_products_f32x2(T, in[0] + i * 36, in[1] + j * 36);
+    } else {
+      // Block (i, k) has the parity of k and block (j, l) that of l, so every
+      // colour block loads as 16-byte vectors.
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      cx<R> x[9];
-      if (k & 1) load9p<true>(x, in[0] + (i * 4 + k) * 9);
-      else load9p<false>(x, in[0] + (i * 4 + k) * 9);
+      for (int k = 0; k < 4; ++k) {
+        cx<R> x[9];
+        if (k & 1) load9p<true>(x, in[0] + (i * 4 + k) * 9);
+        else load9p<false>(x, in[0] + (i * 4 + k) * 9);
 #pragma unroll
-      for (int l = 0; l < 4; ++l) {
-        cx<R> y[9];
-        if (l & 1) load9p<true>(y, in[1] + (j * 4 + l) * 9);
-        else load9p<false>(y, in[1] + (j * 4 + l) * 9);
-        cx<R> t = czero<R>();
+        for (int l = 0; l < 4; ++l) {
+          cx<R> y[9];
+          if (l & 1) load9p<true>(y, in[1] + (j * 4 + l) * 9);
+          else load9p<false>(y, in[1] + (j * 4 + l) * 9);
+          cx<R> t = czero<R>();
 #pragma unroll
-        for (int e = 0; e < 9; ++e) cfma_conj(t, x[e], y[e]);
-        T[k][l] = t;
+          for (int e = 0; e < 9; ++e) cfma_conj(t, x[e], y[e]);
+          T[k][l] = t;
+        }
       }
     }
     // V[b] = i^beta_s(i) sum_l (g5 Gamma(b))^T-phase(l) T[perm_b(l)][l]
@@ -1140,8 +1196,13 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
       S *dst;  // 32-byte aligned
       if constexpr (SPLIT) dst = out + (a >> 3) * sites_per_slice(ps_) * 128 + (a & 7) * 16 + b0;
       else dst = out + a * 16 + b0;
-      st2(dst, mul_phase(X[h][0], alpha), mul_phase(X[h][1], alpha));
-      st2(dst + 2, mul_phase(X[h][2], alpha), mul_phase(X[h][3], alpha));
+      if constexpr (ALPHA) {
+        st2(dst, mul_phase(X[h][0], alpha), mul_phase(X[h][1], alpha));
+        st2(dst + 2, mul_phase(X[h][2], alpha), mul_phase(X[h][3], alpha));
+      } else {
+        st2(dst, X[h][0], X[h][1]);
+        st2(dst + 2, X[h][2], X[h][3]);
+      }
     }
   }
 };
