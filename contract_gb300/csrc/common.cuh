@@ -157,6 +157,56 @@ template <class R> __device__ __forceinline__ cx<R> dot9(const cx<R> x[9], const
   return s;
 }
 
+// Complex64 forms on packed FP32x2 FMAs (one instruction updates both lanes
+// of a (re, im) pair; the issue slots of the products halve).
+//   x * y = x y.x + (i x) y.y: x and i x = (-x.y, x.x) as pairs, y.x and y.y
+//   broadcast to both lanes.
+__device__ __forceinline__ float2 bcast2(float v) { return make_float2(v, v); }
+
+__device__ __forceinline__ void wedge_acc(cx<float> d[9], const cx<float> x[9], const cx<float> y[9])
+{
+  float2 xn[9], xr[9], o[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    xn[q] = make_float2(x[q].x, x[q].y);
+    xr[q] = make_float2(-x[q].y, x[q].x);
+    o[q] = make_float2(d[q].x, d[q].y);
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const int e1 = (e + 1) % 3, e2 = (e + 2) % 3;
+      float2 &t = o[3 * a + e];
+      const cx<float> p = y[3 * a2 + e2], m1 = y[3 * a2 + e1], m2 = y[3 * a1 + e2], p2 = y[3 * a1 + e1];
+      t = __ffma2_rn(xn[3 * a1 + e1], bcast2(p.x), t);
+      t = __ffma2_rn(xr[3 * a1 + e1], bcast2(p.y), t);
+      t = __ffma2_rn(xn[3 * a1 + e2], bcast2(-m1.x), t);
+      t = __ffma2_rn(xr[3 * a1 + e2], bcast2(-m1.y), t);
+      t = __ffma2_rn(xn[3 * a2 + e1], bcast2(-m2.x), t);
+      t = __ffma2_rn(xr[3 * a2 + e1], bcast2(-m2.y), t);
+      t = __ffma2_rn(xn[3 * a2 + e2], bcast2(p2.x), t);
+      t = __ffma2_rn(xr[3 * a2 + e2], bcast2(p2.y), t);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) d[q] = {o[q].x, o[q].y};
+}
+
+// sum x[k] y[k] = (A.x - B.y, A.y + B.x) with A = sum x.x y, B = sum x.y y.
+__device__ __forceinline__ cx<float> dot9(const cx<float> x[9], const cx<float> y[9])
+{
+  float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const float2 yv = make_float2(y[k].x, y[k].y);
+    A = __ffma2_rn(yv, bcast2(x[k].x), A);
+    B = __ffma2_rn(yv, bcast2(x[k].y), B);
+  }
+  return {A.x - B.y, A.y + B.x};
+}
+
 template <class R, class S> __device__ __forceinline__ void load9(cx<R> out[9], const S *blk)
 {
 #pragma unroll
