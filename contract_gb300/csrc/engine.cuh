@@ -121,9 +121,11 @@ template <class Op> constexpr size_t engine_smem_bytes() { return Smem<Op>::BYTE
 
 // FP32 ops ask for two CTAs per SM when their shared memory fits (228 KB per
 // SM, 1 KB reserved per CTA), which caps registers at 128 per thread; FP64 ops
-// are bound by the FP64 pipe and keep one CTA with the full register file.
+// are bound by the FP64 pipe and keep one CTA with the full register file.  An
+// op may ask for more (MIN_CTAS), trading registers for warps.
 template <class Op> constexpr int min_blocks()
 {
+  if constexpr (Op::MIN_CTAS > 0) return Op::MIN_CTAS;
   return (sizeof(typename Op::R) == 4 && 2 * (Smem<Op>::BYTES + sizeof(typename Op::Params) + 1024) <= 233472) ? 2
                                                                                                               : 1;
 }

@@ -67,8 +67,8 @@ cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<dou
                    : run_batch<BaryonFusedCliffOp<double, double2, 4, 16, 2, 2>>(job, p, specs, n);
   }
   const OpParams<float> q = convert_params<float>(p);
-  return nw == 1 ? run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1>>(job, q, specs, n)
-                 : run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2>>(job, q, specs, n);
+  return nw == 1 ? run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3>>(job, q, specs, n)
+                 : run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3>>(job, q, specs, n);
 }
 
 } // namespace cgb

@@ -571,6 +571,8 @@ template <class R_, class S_, int CW_, int TPS_, int NST_> struct OpBase {
   // Field ops: true when site() stores its outputs to global memory itself
   // (the engine then passes the destination, or nullptr for a site to skip).
   static constexpr bool DIRECT_OUT = false;
+  // Resident CTAs per SM that the launch bounds ask for (0: the engine's rule).
+  static constexpr int MIN_CTAS = 0;
   static_assert(32 % TPS_ == 0, "a site's threads must sit in one warp");
 };
 
@@ -650,10 +652,11 @@ struct BaryonFusedCliffOp : OpBase<R, S, CW, TPS, NST> {
 
 // The same six types x NW projectors with both triangle passes in one m loop
 // (fused_merged_site): fewer N loads, more live registers.
-template <class R, class S, int CW, int TPS, int NST, int NW>
+template <class R, class S, int CW, int TPS, int NST, int NW, int MINB = 0>
 struct BaryonFusedCliffMergedOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW);
   static constexpr bool FIELD = false;
+  static constexpr int MIN_CTAS = MINB;
   static_assert(TPS == 16, "one (i, l) pair per thread");
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
