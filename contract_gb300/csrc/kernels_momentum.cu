@@ -185,18 +185,49 @@ __device__ __forceinline__ void zacc(ChunkSum<double> &a, double c, double2 v)
 }
 __device__ __forceinline__ void zacc(ChunkSum<float> &a, float c, float2 v) { a.add(cx<float> {c * v.x, c * v.y}); }
 
-template <class R, int CNT>
+//   TMAP (planes of the fused kernel, which projects the spin-colour products
+//     T[i][j][k][l] instead of the Gamma pairs): each momentum's 256 sums go
+//     through shared memory, rounded to FP32, and output (A, B) is formed as
+//       sum_{j,k} i^(ph_A(j) + ph_B(k)) T[perm_A(j)][j][k][perm_B(k)],
+//     ph_n(r) the phase of (g5 Gamma(n)) at (r, perm_n(r)), in FP32: its
+//     rounding is of the order of the operands' own.
+__constant__ GammaTables kMomGamma = build_gamma_tables();
+
+template <class R, int CNT, bool TMAP>
 __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>::type *__restrict__ planes,
                                                           double2 *__restrict__ out, const __grid_constant__ MomPlan plan)
 {
   const int q = blockIdx.x, t = blockIdx.y, g = threadIdx.x;
   const int lz = plan.latt[2], lt = plan.latt[3];
   __shared__ R cz[kMomMaxL], sz[kMomMaxL];
+  // TMAP staging: product index g at g + g / 16 (rows of 16 padded by one, so
+  // that a warp's gathers below fall in distinct banks)
+  __shared__ float2 tp[TMAP ? CNT : 1][2][272];
+  __shared__ uint8_t gperm[16][4], gph[16][4];
+  if (TMAP && g < 64) {
+    gperm[g >> 2][g & 3] = kMomGamma.perm[g >> 2][g & 3];
+    gph[g >> 2][g & 3] = kMomGamma.ph_g5g_t[g >> 2][g & 3];
+  }
   for (int k = g; k < lz; k += blockDim.x) {
     cz[k] = R(plan.cosz[k]);
     sz[k] = R(plan.sinz[k]);
   }
   __syncthreads();
+  int src[16];        // TMAP: staging index of each of output g's 16 terms
+  uint32_t phs = 0u;  // and their phases, 2 bits each
+  if constexpr (TMAP) {
+    const int A = g >> 4, B = g & 15;
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int ia = gperm[A][jj];
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const int lb = gperm[B][kk];
+        src[jj * 4 + kk] = (kk * 4 + lb) * 17 + (ia ^ jj) * 4 + ia;
+        phs |= ((uint32_t)(gph[A][ia] + gph[B][lb]) & 3u) << (2 * (jj * 4 + kk));
+      }
+    }
+  }
   const int g0 = plan.q_g0[q], g1 = plan.q_g0[q + 1];
   for (int base = g0; base < g1; base += CNT) {
     const int cnt = min(CNT, g1 - base);
@@ -218,29 +249,55 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
         }
       }
     }
+    if constexpr (TMAP) __syncthreads();  // the previous pass's reads of tp are done
 #pragma unroll
     for (int k = 0; k < CNT; ++k) {
       if (k < cnt) {
-        const double2 c = ca[k].value(), sn = sa[k].value();
-        const int pp = plan.gz_plus[base + k], pn = plan.gz_minus[base + k];
-        if (pp >= 0) out[((size_t)pp * lt + t) * 256 + g] = make_double2(c.x - sn.y, c.y + sn.x);
-        if (pn >= 0) out[((size_t)pn * lt + t) * 256 + g] = make_double2(c.x + sn.y, c.y - sn.x);
+        if constexpr (TMAP) {  // FP32 from here on: no FP64-pipe conversions
+          const cx<float> c = ca[k].value_f32(), sn = sa[k].value_f32();
+          tp[k][0][g + (g >> 4)] = make_float2(c.x - sn.y, c.y + sn.x);
+          tp[k][1][g + (g >> 4)] = make_float2(c.x + sn.y, c.y - sn.x);
+        } else {
+          const double2 c = ca[k].value(), sn = sa[k].value();
+          const int pp = plan.gz_plus[base + k], pn = plan.gz_minus[base + k];
+          if (pp >= 0) out[((size_t)pp * lt + t) * 256 + g] = make_double2(c.x - sn.y, c.y + sn.x);
+          if (pn >= 0) out[((size_t)pn * lt + t) * 256 + g] = make_double2(c.x + sn.y, c.y - sn.x);
+        }
+      }
+    }
+    if constexpr (TMAP) {
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < CNT; ++k) {
+        if (k >= cnt) break;
+#pragma unroll
+        for (int sg = 0; sg < 2; ++sg) {
+          const int pm = sg ? plan.gz_minus[base + k] : plan.gz_plus[base + k];
+          if (pm < 0) continue;
+          cx<float> o = czero<float>();
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const float2 v = tp[k][sg][src[e]];
+            o = cadd(o, mul_phase(cx<float> {v.x, v.y}, (phs >> (2 * e)) & 3u));
+          }
+          out[((size_t)pm * lt + t) * 256 + g] = make_double2(o.x, o.y);
+        }
       }
     }
   }
 }
 
-template <class R>
+template <class R, bool TMAP>
 cudaError_t launch_finalize(const Job &job, const typename Vec2<R>::type *planes, double2 *out, const MomPlan &plan)
 {
   int most = 1;  // Z groups of the pair with the most
   for (int q = 0; q < plan.nq; ++q) most = std::max(most, plan.q_g0[q + 1] - plan.q_g0[q]);
   const dim3 grid(plan.nq, plan.latt[3]);
-  if (most <= 1) momentum_finalize<R, 1><<<grid, 256, 0, job.stream>>>(planes, out, plan);
-  else if (most <= 2) momentum_finalize<R, 2><<<grid, 256, 0, job.stream>>>(planes, out, plan);
-  else if (most <= 3) momentum_finalize<R, 3><<<grid, 256, 0, job.stream>>>(planes, out, plan);
-  else if (most <= 4) momentum_finalize<R, 4><<<grid, 256, 0, job.stream>>>(planes, out, plan);
-  else momentum_finalize<R, 8><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  if (most <= 1) momentum_finalize<R, 1, TMAP><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else if (most <= 2) momentum_finalize<R, 2, TMAP><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else if (most <= 3) momentum_finalize<R, 3, TMAP><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else if (most <= 4) momentum_finalize<R, 4, TMAP><<<grid, 256, 0, job.stream>>>(planes, out, plan);
+  else momentum_finalize<R, 8, TMAP><<<grid, 256, 0, job.stream>>>(planes, out, plan);
   return cudaGetLastError();
 }
 
@@ -276,7 +333,7 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   if (fused) {
     cudaError_t e = launch_momentum_fused(job, p.in[0], p.in[1], planes_m, plan);
     if (e != cudaSuccess) return e;
-    return launch_finalize<float>(job, planes_m, static_cast<double2 *>(out), plan);
+    return launch_finalize<float, true>(job, planes_m, static_cast<double2 *>(out), plan);
   }
 
   OpParams<double> q = p;
@@ -305,11 +362,11 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
     }
     e = launch_plane<double, double2>(job, reinterpret_cast<const double2 *>(ws), planes, plan, grid);
     if (e != cudaSuccess) return e;
-    return launch_finalize<double>(job, planes, static_cast<double2 *>(out), plan);
+    return launch_finalize<double, false>(job, planes, static_cast<double2 *>(out), plan);
   }
   e = launch_plane<float, float2>(job, reinterpret_cast<const float2 *>(ws), planes_m, plan, grid);
   if (e != cudaSuccess) return e;
-  return launch_finalize<float>(job, planes_m, static_cast<double2 *>(out), plan);
+  return launch_finalize<float, false>(job, planes_m, static_cast<double2 *>(out), plan);
 }
 
 } // namespace cgb

@@ -1,28 +1,30 @@
 // Fused all-gamma meson momentum projection, mixed form (complex64 storage,
-// FP32 arithmetic): the per-site 16 x 16 meson values and the X and Y
-// transforms of the separable projection in one kernel, so the 256 complex
-// values per site live only in shared memory.  The three-kernel form writes
-// them to HBM (2 KB per site) and reads them back; here HBM traffic is the
-// two propagators (2 x 1152 B per site) plus one FP64 plane per (t, z).
+// FP32 arithmetic): the per-site spin-colour products behind the 16 x 16 meson
+// values and the X and Y transforms of the separable projection in one
+// kernel, so the 256 complex values per site live only in shared memory.  The
+// three-kernel form writes the meson values to HBM (2 KB per site) and reads
+// them back; here HBM traffic is the two propagators (2 x 1152 B per site)
+// plus one FP32 plane per (t, z).
 //
 // One persistent CTA per SM walks (t, z) planes.  A plane's sites are taken
 // in row order -- for each y, both parities' half-rows -- in tiles of 16:
 //
 //   warps 0-7    site warps: each fetches its own two sites of a tile with
 //                cp.async.bulk into a per-warp kFNst-stage ring (its own full
-//                mbarriers, kFNst - 1 tiles ahead), runs MesonAllGammaOp on
-//                them and leaves the 256 values per site in one of two shared
-//                output buffers (ofull / oempty mbarriers)
-//   warps 8-15   transform warps: thread g owns gamma pair g; for each site of
+//                mbarriers, kFNst - 1 tiles ahead), forms their 256 spin-colour
+//                products T (site_products) and leaves them in one of two
+//                shared output buffers (ofull / oempty mbarriers)
+//   warps 8-15   transform warps: thread g owns product g; for each site of
 //                a row, C += cos(k x) v and S += sin(k x) v per X group; at
 //                the end of a row G(nx) -> shared column, then
 //                H[q] += exp(i ky y) G(nx(q)) for every (nx, ny) pair q
 //
 // Sixteen warps (no separate producer) leave 128 registers per thread.  At the
-// end of a plane each transform thread writes H[q] in FP64 to the plane
-// buffer; momentum_finalize applies the Z transform in FP64, as in the
-// three-kernel form.  Every mbarrier wait is bounded in wall time; a timed-out
-// wait reports kDevErrWaitTimeout, raises the CTA's abort flag and returns.
+// end of a plane each transform thread writes H[q] (FP32) to the plane buffer;
+// momentum_finalize applies the Z transform with a compensated sum, then the
+// product -> Gamma-pair combination, and returns FP64.  Every mbarrier wait is
+// bounded in wall time; a timed-out wait reports kDevErrWaitTimeout, raises
+// the CTA's abort flag and returns.
 #include "engine.cuh"
 #include "momentum.hpp"
 
@@ -30,8 +32,27 @@ namespace cgb {
 
 namespace {
 
-// without the per-class phase, which the transform applies to its plane sums
-using FusedSiteOp = MesonAllGammaOp<float, float2, 8, 2, false, false>;
+// The 256 spin-colour products of a site,
+//   T[i][j][k][l] = sum_c S1[i][k][c] conj(S2[j][l][c]),
+// from which every Gamma pair is a signed sum of 16 (see momentum_finalize).
+// That combination is linear and the same at every site, so it commutes with
+// the projection: the kernel projects T, and the finalize applies it once per
+// momentum and timeslice instead of once per site.  Thread sub = 4 s + i of a
+// site computes the 16 products of (i, j = i ^ s) and stores T[k][l] at index
+// (4 k + l) * 16 + sub, so a warp's stores and the transform's loads are
+// consecutive.
+__device__ __forceinline__ void site_products(const float2 *in0, const float2 *in1, int sub, float2 *dst)
+{
+  const int s = sub >> 2, i = sub & 3, j = i ^ s;
+  cx<float> T[4][4];
+  conj_products_f32x2(T, in0 + i * 36, in1 + j * 36);
+  if (!dst) return;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) dst[(k * 4 + l) * 16 + sub] = make_float2(T[k][l].x, T[k][l].y);
+}
+
 constexpr int kFCW = 8;                           // site warps (and transform warps)
 constexpr int kFSites = kFCW * 2;                 // sites per tile (16 threads per site)
 constexpr int kFNst = 3;                          // input ring stages
@@ -49,7 +70,6 @@ struct FusedArgs {
   float2 *planes;     // [Lt][Lz][nq][256], FP32 sums
   DeviceStatus *status;
   int tiles_per_plane;
-  OpParams<float> op;  // the site op's parameter block (unused by the non-split form)
 };
 
 static_assert(sizeof(FusedArgs) + sizeof(MomPlan) <= 32764, "kernel parameters exceed 32764 bytes");
@@ -156,7 +176,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
       const float2 *in[2] = {reinterpret_cast<const float2 *>(sb + (size_t)site * FL::SLOT),
                              reinterpret_cast<const float2 *>(sb + ((size_t)kFSites + site) * FL::SLOT)};
       float2 *dst = site < n ? obuf + ((size_t)ob * kFSites + site) * 256 : nullptr;
-      FusedSiteOp::site(a.op, in, nullptr, sub, dst);
+      site_products(in[0], in[1], sub, dst);
       __threadfence_block();
       __syncwarp();
       if (lane == 0) mbar_arrive(&ofull[ob]);
@@ -168,7 +188,6 @@ __global__ void __launch_bounds__(kFThreads, 1)
   const int g = threadIdx.x - 32 * kFCW;
   const int half = lx >> 1;
   const bool aligned = half % kFSites == 0;  // every tile lies in one half-row
-  const uint32_t alpha = class_alpha(g >> 4);
   const bool zero0 = plan.gx_k[0] == 0;      // X group 0 is nx = 0: C = sum v, S = 0
   cx<float> *gxs = reinterpret_cast<cx<float> *>(smem + kFGxOff);  // [kMomMaxPx][256], column g is this thread's
   int u = 0;
@@ -216,7 +235,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
         const int r0 = (k * kFSites) % lx, par = r0 >= half ? 1 : 0;
         const int x0 = 2 * (r0 - par * half) + ((par + t + z + y) & 1);
         if (zero0) {
-#pragma unroll
+#pragma unroll 8
           for (int s = 0; s < kFSites; ++s) {
             const cx<float> v = col[s * 256];
             gc[0].x += v.x;
@@ -225,7 +244,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
             for (int gi = 1; gi < NG; ++gi) xstep(gi, phx[gi][x0 + 2 * s][0], phx[gi][x0 + 2 * s][1], v);
           }
         } else {
-#pragma unroll
+#pragma unroll 8
           for (int s = 0; s < kFSites; ++s) {
             const cx<float> v = col[s * 256];
 #pragma unroll
@@ -252,10 +271,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
     }
 #pragma unroll
     for (int q = 0; q < QC; ++q)
-      if (q < plan.nq) {
-        const cx<float> v = mul_phase(h[q], alpha);
-        a.planes[((size_t)unit * plan.nq + q) * 256 + g] = make_float2(v.x, v.y);
-      }
+      if (q < plan.nq) a.planes[((size_t)unit * plan.nq + q) * 256 + g] = make_float2(h[q].x, h[q].y);
   }
 }
 
