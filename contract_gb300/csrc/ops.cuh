@@ -1003,7 +1003,7 @@ __device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[4][4], const 
   for (int k = 0; k < 4; ++k)
 #pragma unroll
     for (int l = 0; l < 4; ++l) acc[k][l] = make_float2(0.f, 0.f);
-#pragma unroll
+#pragma unroll 3  // fully unrolled, the loads of later colours run ahead and spill at 128 registers
   for (int e = 0; e < 9; ++e) {
     float2 a[4], ar[4], b[4];
 #pragma unroll
