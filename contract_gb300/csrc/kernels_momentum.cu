@@ -213,21 +213,6 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
     sz[k] = R(plan.sinz[k]);
   }
   __syncthreads();
-  int src[16];        // TMAP: staging index of each of output g's 16 terms
-  uint32_t phs = 0u;  // and their phases, 2 bits each
-  if constexpr (TMAP) {
-    const int A = g >> 4, B = g & 15;
-#pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-      const int ia = gperm[A][jj];
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        const int lb = gperm[B][kk];
-        src[jj * 4 + kk] = (kk * 4 + lb) * 17 + (ia ^ jj) * 4 + ia;
-        phs |= ((uint32_t)(gph[A][ia] + gph[B][lb]) & 3u) << (2 * (jj * 4 + kk));
-      }
-    }
-  }
   const int g0 = plan.q_g0[q], g1 = plan.q_g0[q + 1];
   for (int base = g0; base < g1; base += CNT) {
     const int cnt = min(CNT, g1 - base);
@@ -238,14 +223,23 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
       kk[k] = 0;
       step[k] = k < cnt ? plan.gz_k[base + k] : 0;
     }
-    for (int z = 0; z < lz; ++z) {
-      const auto v = planes[((size_t)(t * lz + z) * plan.nq + q) * 256 + g];
+    using V2 = typename Vec2<R>::type;
+    constexpr int ZB = 4;  // plane loads in flight per thread
+    for (int z0 = 0; z0 < lz; z0 += ZB) {
+      V2 v[ZB];
 #pragma unroll
-      for (int k = 0; k < CNT; ++k) {
-        if (k < cnt) {
-          zacc(ca[k], cz[kk[k]], v);
-          zacc(sa[k], sz[kk[k]], v);
-          if ((kk[k] += step[k]) >= lz) kk[k] -= lz;  // k * z mod Lz
+      for (int u = 0; u < ZB; ++u)
+        if (z0 + u < lz) v[u] = planes[((size_t)(t * lz + z0 + u) * plan.nq + q) * 256 + g];
+#pragma unroll
+      for (int u = 0; u < ZB; ++u) {
+        if (z0 + u >= lz) break;
+#pragma unroll
+        for (int k = 0; k < CNT; ++k) {
+          if (k < cnt) {
+            zacc(ca[k], cz[kk[k]], v[u]);
+            zacc(sa[k], sz[kk[k]], v[u]);
+            if ((kk[k] += step[k]) >= lz) kk[k] -= lz;  // k * z mod Lz
+          }
         }
       }
     }
@@ -267,6 +261,19 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
     }
     if constexpr (TMAP) {
       __syncthreads();
+      int src[16];        // staging index of each of output g's 16 terms
+      uint32_t phs = 0u;  // and their phases, 2 bits each
+      const int A = g >> 4, B = g & 15;
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) {
+        const int ia = gperm[A][jj];
+#pragma unroll
+        for (int kb = 0; kb < 4; ++kb) {
+          const int lb = gperm[B][kb];
+          src[jj * 4 + kb] = (kb * 4 + lb) * 17 + (ia ^ jj) * 4 + ia;
+          phs |= ((uint32_t)(gph[A][ia] + gph[B][lb]) & 3u) << (2 * (jj * 4 + kb));
+        }
+      }
 #pragma unroll
       for (int k = 0; k < CNT; ++k) {
         if (k >= cnt) break;
