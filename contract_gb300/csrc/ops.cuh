@@ -727,6 +727,28 @@ struct MesonOp : OpBase<R, S, CW, TPS, NST> {
   }
 };
 
+// x . conj(y) over a colour block.  Complex64: packed FP32x2 FMAs on two
+// accumulators, A = sum x.re y and B = sum x.im y (y as a pair, x broadcast),
+// then (A.x + B.y, B.x - A.y): no operand needs reordering.
+template <class R> __device__ __forceinline__ cx<R> conj_dot9(const cx<R> x[9], const cx<R> y[9])
+{
+  cx<R> t = czero<R>();
+#pragma unroll
+  for (int e = 0; e < 9; ++e) cfma_conj(t, x[e], y[e]);
+  return t;
+}
+template <> __device__ __forceinline__ cx<float> conj_dot9<float>(const cx<float> x[9], const cx<float> y[9])
+{
+  float2 A = make_float2(0.f, 0.f), B = A;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    const float2 yv = make_float2(y[e].x, y[e].y);
+    A = __ffma2_rn(yv, bcast2(x[e].x), A);
+    B = __ffma2_rn(yv, bcast2(x[e].y), B);
+  }
+  return {A.x + B.y, B.x - A.y};
+}
+
 template <class R> __device__ __forceinline__ cx<R> pick4(const cx<R> t[4], int k)
 {
   return k == 0 ? t[0] : (k == 1 ? t[1] : (k == 2 ? t[2] : t[3]));
@@ -755,9 +777,7 @@ struct MesonAllSourceOp : OpBase<R, S, CW, 4, NST> {
         cx<R> x[9];
         if (k & 1) load9p<true>(x, in[0] + (i * 4 + k) * 9);
         else load9p<false>(x, in[0] + (i * 4 + k) * 9);
-        t[k] = czero<R>();
-#pragma unroll
-        for (int e = 0; e < 9; ++e) cfma_conj(t[k], x[e], y[e]);
+        t[k] = conj_dot9<R>(x, y);
       }
 #pragma unroll
       for (int g = 0; g < 16; ++g) vals[g] = cadd(vals[g], mul_phase(pick4(t, G.perm[g][l]), G.ph_g5g_t[g][l]));
@@ -785,11 +805,10 @@ struct MesonAllSinkOp : OpBase<R, S, CW, 4, NST> {
       cx<R> t[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        t[j] = czero<R>();
-        const S *x = in[0] + (i * 4 + k) * 9;
-        const S *y = in[1] + (j * 4 + l) * 9;
-#pragma unroll
-        for (int e = 0; e < 9; ++e) cfma_conj(t[j], ld<R>(x + e), ld<R>(y + e));
+        cx<R> x[9], y[9];
+        load9(x, in[0] + (i * 4 + k) * 9);
+        load9(y, in[1] + (j * 4 + l) * 9);
+        t[j] = conj_dot9<R>(x, y);
       }
 #pragma unroll
       for (int g = 0; g < 16; ++g) vals[g] = cadd(vals[g], mul_phase(pick4(t, G.perm[g][i]), G.ph_g5g_t[g][i]));
