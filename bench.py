@@ -363,7 +363,7 @@ def run_ours(args, world, rank, local):
             "hbm_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "scalar_kernel<BaryonFusedCliffMergedOp<float,float2,4,16,2,2>> + finalize_kernel",
+                         "kernel": "scalar_kernel<BaryonFusedCliffMergedOp<float,float2,4,16,2,2,3>> + finalize_kernel",
                          "algorithmic_bytes_per_launch": bytes_per_launch},
             "fp32_pipe": {"achieved_tflops": flops_per_launch / (ms_mixed * 1e-3) / 1e12,
                           "peak_tflops": 73.1, "peak_source": "measured FFMA probe",
