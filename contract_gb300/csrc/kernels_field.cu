@@ -22,9 +22,10 @@ static cudaError_t seq_dispatch(const Job &job, bool loop, int role, const OpPar
 }
 
 // complex64 variants: the two-CTA shapes keep more tiles (and stores) in flight.
-static const VariantSet<float, 2> kDiquarkM = {
-  {run_field<DiquarkOp<float, float2, 6, 16, 2>>, run_field<DiquarkOp<float, float2, 8, 16, 3>>},
-  {"cw6.tps16.st2", "cw8.tps16.st3"},
+static const VariantSet<float, 4> kDiquarkM = {
+  {run_field<DiquarkOp<float, float2, 6, 16, 2>>, run_field<DiquarkOp<float, float2, 8, 16, 3>>,
+   run_field<DiquarkOp<float, float2, 6, 16, 2, true>>, run_field<DiquarkOp<float, float2, 8, 16, 3, true>>},
+  {"cw6.tps16.st2", "cw8.tps16.st3", "cw6.tps16.st2.direct", "cw8.tps16.st3.direct"},
   0};
 
 cudaError_t launch_diquark(const Job &job, const OpParams<double> &p)

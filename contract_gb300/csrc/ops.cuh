@@ -823,10 +823,13 @@ struct MesonAllSinkOp : OpBase<R, S, CW, 4, NST> {
 // Diquark (include/diquark.cuh:33-57):
 //   D[m][l][ad] = g5[m] g5[l] conj( c2(l) sum_i c1(i) (P_i[i][perm2 l] ^ P_j[perm1 i][m])[ad] )
 // with c1 from Gamma_ij, c2 from Gamma_kl^T.  Thread handles 16/TPS blocks (m, l).
-template <class R, class S, int CW, int TPS, int NST>
+template <class R, class S, int CW, int TPS, int NST, bool DIRECT = false>
 struct DiquarkOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 144;
   static constexpr bool FIELD = true;
+  // DIRECT: each thread stores its blocks straight to HBM (72 contiguous bytes
+  // a block) instead of staging the site in shared memory for a bulk store.
+  static constexpr bool DIRECT_OUT = DIRECT;
   __device__ static long long out_index(const OpParams<R> &, long long site) { return site; }
   __device__ static S *out_ptr(const OpParams<R> &, long long d, S *base) { return base + d * OUT_ELEMS; }
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *, int sub, S *out)

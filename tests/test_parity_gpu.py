@@ -248,6 +248,35 @@ def test_meson_momentum_fused_tiles(api, latt):
     api.check_device()
 
 
+def test_meson_momentum_many_z_groups(api):
+    """Ten +nz/-nz groups for one (nx, ny) pair: the finalize runs two passes over
+    its groups, each staging the projected products for the Gamma-pair combination."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    latt = (4, 4, 20, 2)
+    moms = np.array([[0, 0, n] for n in range(-9, 11)], dtype=np.int32)  # nz = 10 is its own negative
+    pi = eo.make_propagator(latt, 71, 0.2)
+    pj = eo.make_propagator(latt, 72, 0.3)
+    site = eo.meson_all_gamma(pi, pj).reshape(256, -1)
+    ref = eo.momentum_project(site, latt, moms).transpose(1, 2, 0)
+    sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real).T[None]
+    for prec, tol in ((0, TOL_C128), (1, TOL_C64_TIMESLICE)):
+        a, b = cuda(pi, prec >= 1), cuda(pj, prec >= 1)
+        out = torch.full((len(moms), latt[3], 256), float("nan"), dtype=torch.complex128, device="cuda")
+        lib.contract_meson_all_gamma_momentum(out.data_ptr(), a.data_ptr(), b.data_ptr(), pi.shape[0],
+                                              (ctypes.c_int * 4)(*latt),
+                                              moms.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(moms), prec)
+        got = out.cpu().numpy()
+        assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+        if prec == 0:
+            assert rel_err(got, ref) < tol
+        else:
+            assert (np.abs(got - ref) / np.maximum(np.abs(ref), sig)).max() < tol
+    api.check_device()
+
+
 def test_momentum_tensor_cores_two_momentum_groups(api):
     """CONTRACT_C64_TC with 147 momenta (two groups of 128 GEMM rows) on a
     lattice whose timeslice (6 x 6 x 4 = 144 sites) spans 18 k-steps."""
