@@ -1161,7 +1161,10 @@ void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const
   OpParams<double> p {};
   p.in[0] = propag_i;
   p.in[1] = propag_j;
-  cuda_ok(cgb::launch_meson_momentum(job, p, plan, correl, tensor_cores), "contract_meson_all_gamma_momentum");
+  const int aux = tensor_cores ? 2 : (job.prec == cgb::Prec::C64 && cgb::momentum_fused_supported(plan) ? 1 : 0);
+  cuda_ok(tuned_launch(cgb::Kind::Momentum, job, aux,
+                       [&](const cgb::Job &j) { return cgb::launch_meson_momentum(j, p, plan, correl, tensor_cores); }),
+          "contract_meson_all_gamma_momentum");
 }
 
 void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,

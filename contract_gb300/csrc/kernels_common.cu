@@ -1,5 +1,6 @@
 // Per-timeslice finalisation and precision conversion kernels.
 #include "launch_impl.cuh"
+#include "momentum.hpp"
 
 namespace cgb {
 
@@ -60,6 +61,7 @@ int launch_variants(Kind kind, Prec prec, int aux, const char *const **names)
   case Kind::Diquark: return field_variants(prec, false, names);
   case Kind::Sequential: return field_variants(prec, true, names);
   case Kind::MesonAll: return meson_all_variants(prec, aux != 0, names);
+  case Kind::Momentum: return momentum_variants(prec, aux, names);
   }
   return 1;
 }

@@ -319,16 +319,37 @@ static bool fused_disabled()
   return off;
 }
 
+static const char *const kMomFusedNames[] = {"fused.site8.xy8", "three-kernel"};
+static const char *const kMomTcNames[] = {"tc.unit512", "tc.unit256", "tc.unit1024"};
+static const int kMomTcSteps[] = {512, 256, 1024};
+
+int momentum_variants(Prec prec, int aux, const char *const **names)
+{
+  if (aux >= 2 && prec == Prec::C64) {
+    *names = kMomTcNames;
+    return 3;
+  }
+  if (aux == 1 && prec == Prec::C64) {
+    *names = kMomFusedNames;
+    return 2;
+  }
+  return 1;
+}
+
 cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, const MomPlan &plan, void *out,
                                   bool tensor_cores)
 {
   if (job.volume == 0) return cudaSuccess;
   if (tensor_cores && job.prec != Prec::C64) return cudaErrorInvalidValue;
-  const bool fused = !tensor_cores && job.prec == Prec::C64 && momentum_fused_supported(plan) && !fused_disabled();
+  // job.variant (autotuner): complex64 -- 1 runs the three-kernel form; tensor
+  // cores -- the k-steps per work unit
+  const bool fused = !tensor_cores && job.prec == Prec::C64 && momentum_fused_supported(plan) && !fused_disabled() &&
+                     job.variant != 1;
   const size_t elem = job.prec == Prec::C128 ? sizeof(double2) : sizeof(float2);
   const size_t c_bytes = fused ? 0 : ((size_t)job.volume * 256 * elem + 255) / 256 * 256;
   const int lz = plan.latt[2], lt = plan.latt[3];
-  const TcGeom tg = make_tc_geom(plan);
+  const int tcv = tensor_cores && job.variant >= 0 && job.variant < 3 ? job.variant : 0;
+  const TcGeom tg = make_tc_geom(plan, kMomTcSteps[tcv]);
   const size_t a_bytes = (tc_phase_bytes(tg) + 255) / 256 * 256;
   const size_t plane_bytes = tensor_cores ? a_bytes + tc_partial_bytes(tg)
                                           : (size_t)lt * lz * plan.nq * 256 * 2 * (job.prec == Prec::C128 ? 8 : 4);

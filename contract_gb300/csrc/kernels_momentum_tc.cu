@@ -477,13 +477,13 @@ __global__ void __launch_bounds__(256) momentum_tc_reduce(const float *__restric
 
 } // namespace
 
-TcGeom make_tc_geom(const MomPlan &plan)
+TcGeom make_tc_geom(const MomPlan &plan, int unit_steps)
 {
   TcGeom g {};
   g.v3 = (long long)plan.latt[0] * plan.latt[1] * plan.latt[2];
   g.lt = plan.latt[3];
   g.j = (int)((g.v3 + 7) / 8);
-  g.ku = g.j < kTcUnitSteps ? g.j : kTcUnitSteps;
+  g.ku = g.j < unit_steps ? g.j : unit_steps;
   g.jb = (g.j + g.ku - 1) / g.ku;
   g.mg = (plan.np + 127) / 128;
   g.units = g.mg * g.jb * g.lt * 2;

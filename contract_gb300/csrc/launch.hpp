@@ -34,7 +34,16 @@ struct Job {
 
 // Ops whose launchers offer several compiled tile shapes (consumer warps,
 // threads per site, ring stages); the autotuner in abi.cpp picks among them.
-enum class Kind { Meson = 0, BaryonLoop = 1, BaryonTri = 2, BaryonFused = 3, Diquark = 4, Sequential = 5, MesonAll = 6 };
+enum class Kind {
+  Meson = 0,
+  BaryonLoop = 1,
+  BaryonTri = 2,
+  BaryonFused = 3,
+  Diquark = 4,
+  Sequential = 5,
+  MesonAll = 6,
+  Momentum = 7
+};
 
 // Number of variants (and their names) for an op at a precision; `aux` is
 // the projector count for BaryonFused and, for BaryonTri, 0 for the

@@ -30,7 +30,8 @@ struct MomPlan {
 };
 
 // Geometry of the tensor-core projection (kernels_momentum_tc.cu): k-steps of
-// 8 sites per timeslice, k-steps per work unit, units.
+// 8 sites per timeslice, k-steps per work unit (a tile-shape choice: 512 by
+// default, 256 and 1024 as autotuner variants), units.
 constexpr int kTcUnitSteps = 512;
 struct TcGeom {
   long long v3;  // sites per timeslice
@@ -41,7 +42,7 @@ struct TcGeom {
   int mg;        // momentum groups of 128
   int units;     // mg * jb * lt * 2
 };
-TcGeom make_tc_geom(const MomPlan &plan);
+TcGeom make_tc_geom(const MomPlan &plan, int unit_steps = kTcUnitSteps);
 size_t tc_phase_bytes(const TcGeom &g);
 size_t tc_partial_bytes(const TcGeom &g);
 cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom &g, const void *field,
@@ -53,6 +54,11 @@ cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom
 bool momentum_fused_supported(const MomPlan &plan);
 cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *in_j, float2 *planes,
                                   const MomPlan &plan);
+
+// Tile-shape variants of the projection for the autotuner (Kind::Momentum).
+// aux = 2 * tensor_cores + (fused form supported):
+//   1: complex64 fused (default) or three kernels; 2, 3: tensor-core unit sizes.
+int momentum_variants(Prec prec, int aux, const char *const **names);
 
 // All-gamma meson correlators at the plan's momenta: out[p][t][16*16]
 // complex128 (device).  Uses job.ws for the per-site values and the plane
