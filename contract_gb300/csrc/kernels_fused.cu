@@ -15,27 +15,29 @@ using Fused2M = BaryonFusedOp<float, float2, 8, 16, 2, 2>;
 
 // complex64, FP32-issue bound: consumer warps per SM vs registers per thread; the
 // merged variants run both triangle passes in one m loop (fewer N loads, more registers).
-static const VariantSet<float, 7> kFusedCliff1M = {
+static const VariantSet<float, 8> kFusedCliff1M = {
   {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 1, 4>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 5, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 7, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 5, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 3, 16, 3, 1>>},
-  {"merged.cw4.tps16.st2.occ3", "merged.cw4.tps16.st2", "merged.cw5.tps16.st2", "merged.cw3.tps16.st2",
-   "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
+  {"merged.cw4.tps16.st2.occ3", "merged.cw3.tps16.st2.occ4", "merged.cw4.tps16.st2", "merged.cw5.tps16.st2",
+   "merged.cw3.tps16.st2", "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
   0};
-static const VariantSet<float, 7> kFusedCliff2M = {
+static const VariantSet<float, 8> kFusedCliff2M = {
   {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 2, 4>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 5, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 7, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 5, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 3, 16, 3, 2>>},
-  {"merged.cw4.tps16.st2.occ3", "merged.cw4.tps16.st2", "merged.cw5.tps16.st2", "merged.cw3.tps16.st2",
-   "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
+  {"merged.cw4.tps16.st2.occ3", "merged.cw3.tps16.st2.occ4", "merged.cw4.tps16.st2", "merged.cw5.tps16.st2",
+   "merged.cw3.tps16.st2", "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
   0};
 
 cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &p)

@@ -29,7 +29,8 @@ template <> struct Vec2<float> { using type = float2; };
 
 using MesonAllGammaP = MesonAllGammaOp<double, double2, 4, 3>;
 using MesonAllGammaM = MesonAllGammaOp<float, float2, 8, 2>;
-using MesonAllGammaSplitM = MesonAllGammaOp<float, float2, 8, 2, true>;  // field of the tensor-core path
+// field of the tensor-core path: the spin-colour products, pair halves apart
+using MesonProductsSplitM = MesonAllGammaOp<float, float2, 8, 2, true, true>;
 
 // One CTA per (z, t, chunk of (nx, ny) pairs); one thread per gamma pair.
 // X transform: NG groups of +nx / -nx (C = sum cos * v, S = sum sin * v; the
@@ -187,11 +188,70 @@ __device__ __forceinline__ void zacc(ChunkSum<float> &a, float c, float2 v) { a.
 
 //   TMAP (planes of the fused kernel, which projects the spin-colour products
 //     T[i][j][k][l] instead of the Gamma pairs): each momentum's 256 sums go
-//     through shared memory, rounded to FP32, and output (A, B) is formed as
-//       sum_{j,k} i^(ph_A(j) + ph_B(k)) T[perm_A(j)][j][k][perm_B(k)],
-//     ph_n(r) the phase of (g5 Gamma(n)) at (r, perm_n(r)), in FP32: its
-//     rounding is of the order of the operands' own.
+//     through shared memory, rounded to FP32, and become the Gamma pairs
+//     (pair_from_products).
 __constant__ GammaTables kMomGamma = build_gamma_tables();
+
+// Gamma pair (A, B) = g from the 256 projected products:
+//   sum_{j,k} i^(ph_A(j) + ph_B(k)) T[perm_A(j)][j][k][perm_B(k)],
+// ph_n(r) the phase of (g5 Gamma(n)) at (r, perm_n(r)), in FP32 (its rounding
+// is of the order of the operands' own).  Products are staged at
+// index p + p / 16 (rows of 16 padded by one against bank conflicts);
+// pair_terms gives each term's staging index and phase.
+struct PairTerms {
+  int src[16];
+  uint32_t phs;  // 2 bits per term
+};
+__device__ __forceinline__ PairTerms pair_terms(const uint8_t (*gperm)[4], const uint8_t (*gph)[4], int g)
+{
+  PairTerms t;
+  t.phs = 0u;
+  const int A = g >> 4, B = g & 15;
+#pragma unroll
+  for (int jj = 0; jj < 4; ++jj) {
+    const int ia = gperm[A][jj];
+#pragma unroll
+    for (int kb = 0; kb < 4; ++kb) {
+      const int lb = gperm[B][kb];
+      t.src[jj * 4 + kb] = (kb * 4 + lb) * 17 + (ia ^ jj) * 4 + ia;
+      t.phs |= ((uint32_t)(gph[A][ia] + gph[B][lb]) & 3u) << (2 * (jj * 4 + kb));
+    }
+  }
+  return t;
+}
+__device__ __forceinline__ cx<float> pair_from_products(const float2 *staged, const PairTerms &t)
+{
+  cx<float> o = czero<float>();
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    const float2 v = staged[t.src[e]];
+    o = cadd(o, mul_phase(cx<float> {v.x, v.y}, (t.phs >> (2 * e)) & 3u));
+  }
+  return o;
+}
+
+// In place over rows of 256 (one (momentum, timeslice) each): projected
+// products -> Gamma pairs.  Used after the tensor-core projection of products.
+__global__ void __launch_bounds__(256) pair_map_kernel(double2 *__restrict__ rows, long long nrows)
+{
+  const int g = threadIdx.x;
+  __shared__ float2 tp[272];
+  __shared__ uint8_t gperm[16][4], gph[16][4];
+  if (g < 64) {
+    gperm[g >> 2][g & 3] = kMomGamma.perm[g >> 2][g & 3];
+    gph[g >> 2][g & 3] = kMomGamma.ph_g5g_t[g >> 2][g & 3];
+  }
+  __syncthreads();
+  const PairTerms terms = pair_terms(gperm, gph, g);
+  for (long long r = blockIdx.x; r < nrows; r += gridDim.x) {
+    const double2 v = rows[r * 256 + g];
+    __syncthreads();  // the previous row's reads of tp are done
+    tp[g + (g >> 4)] = make_float2(float(v.x), float(v.y));
+    __syncthreads();
+    const cx<float> o = pair_from_products(tp, terms);
+    rows[r * 256 + g] = make_double2(o.x, o.y);
+  }
+}
 
 template <class R, int CNT, bool TMAP>
 __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>::type *__restrict__ planes,
@@ -261,19 +321,7 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
     }
     if constexpr (TMAP) {
       __syncthreads();
-      int src[16];        // staging index of each of output g's 16 terms
-      uint32_t phs = 0u;  // and their phases, 2 bits each
-      const int A = g >> 4, B = g & 15;
-#pragma unroll
-      for (int jj = 0; jj < 4; ++jj) {
-        const int ia = gperm[A][jj];
-#pragma unroll
-        for (int kb = 0; kb < 4; ++kb) {
-          const int lb = gperm[B][kb];
-          src[jj * 4 + kb] = (kb * 4 + lb) * 17 + (ia ^ jj) * 4 + ia;
-          phs |= ((uint32_t)(gph[A][ia] + gph[B][lb]) & 3u) << (2 * (jj * 4 + kb));
-        }
-      }
+      const PairTerms terms = pair_terms(gperm, gph, g);
 #pragma unroll
       for (int k = 0; k < CNT; ++k) {
         if (k >= cnt) break;
@@ -281,12 +329,7 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
         for (int sg = 0; sg < 2; ++sg) {
           const int pm = sg ? plan.gz_minus[base + k] : plan.gz_plus[base + k];
           if (pm < 0) continue;
-          cx<float> o = czero<float>();
-#pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            const float2 v = tp[k][sg][src[e]];
-            o = cadd(o, mul_phase(cx<float> {v.x, v.y}, (phs >> (2 * e)) & 3u));
-          }
+          const cx<float> o = pair_from_products(tp[k][sg], terms);
           out[((size_t)pm * lt + t) * 256 + g] = make_double2(o.x, o.y);
         }
       }
@@ -369,12 +412,18 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   for (int k = 0; k < 4; ++k) q.latt[k] = plan.latt[k];
   cudaError_t e;
   if (job.prec == Prec::C128) e = run_field<MesonAllGammaP>(job, q);
-  else if (tensor_cores) e = run_field<MesonAllGammaSplitM>(job, convert_params<float>(q));
+  else if (tensor_cores) e = run_field<MesonProductsSplitM>(job, convert_params<float>(q));
   else e = run_field<MesonAllGammaM>(job, convert_params<float>(q));
   if (e != cudaSuccess) return e;
-  if (tensor_cores)
-    return launch_momentum_tc(job, plan, tg, ws, reinterpret_cast<unsigned char *>(ws + c_bytes),
-                              reinterpret_cast<float *>(ws + c_bytes + a_bytes), out);
+  if (tensor_cores) {
+    e = launch_momentum_tc(job, plan, tg, ws, reinterpret_cast<unsigned char *>(ws + c_bytes),
+                           reinterpret_cast<float *>(ws + c_bytes + a_bytes), out);
+    if (e != cudaSuccess) return e;
+    const long long nrows = (long long)plan.np * lt;
+    const int grid = (int)std::min<long long>(nrows, (long long)job.num_sms * 8);
+    pair_map_kernel<<<grid, 256, 0, job.stream>>>(static_cast<double2 *>(out), nrows);
+    return cudaGetLastError();
+  }
 
   const dim3 grid(lz, lt, (plan.nq + kMomQChunk - 1) / kMomQChunk);
   if (job.prec == Prec::C128) {

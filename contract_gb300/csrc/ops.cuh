@@ -1091,26 +1091,20 @@ CGB_HD constexpr ClassWalsh class_walsh()
 }
 static_assert(class_walsh().ok, "gamma classes must have the Walsh phase structure");
 
-// The phase i^alpha that MesonAllGammaOp applies to every output of first
-// gamma index a.
-CGB_HD constexpr uint32_t class_alpha(int a)
-{
-  constexpr ClassWalsh W = class_walsh();
-  uint32_t al = 0;
-  for (int idx = 0; idx < 16; ++idx)
-    if ((int)((W.member >> (4 * idx)) & 15u) == a) al = (W.alpha >> (2 * idx)) & 3u;
-  return al;
-}
-
 // SPLIT selects the layout [t][pair half][site][128 pairs] (pairs 0-127 and
 // 128-255 of a timeslice in separate planes) that the tensor-core projection
 // streams as contiguous 8-site tiles; otherwise [t][site][256 pairs].
-// ALPHA = false leaves out the constant phase i^alpha of each first-gamma
-// index a (class_alpha(a)); a linear consumer applies it once to its sums.
-template <class R, class S, int CW, int NST, bool SPLIT = false, bool ALPHA = true>
+// PRODUCTS (complex64): store the 256 spin-colour products
+//   T[i][j][k][l] = sum_c S1[i][k][c] conj(S2[j][l][c])
+// instead of the Gamma pairs, product (i, j = i ^ s, k, l) at index
+// (4 k + l) * 16 + 4 s + i.  Each pair is a signed sum of 16 products, the same
+// at every site, so a linear consumer (the momentum projection) forms the pairs
+// once from its sums (pair_from_products in kernels_momentum.cu).
+template <class R, class S, int CW, int NST, bool SPLIT = false, bool PRODUCTS = false>
 struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
   static constexpr int NIN = 2, EXTRA_BYTES = 0, OUT_ELEMS = 256;
   static constexpr bool FIELD = true;
+  static_assert(!PRODUCTS || sizeof(R) == 4, "the product form is complex64 only");
   // Each thread's 16 outputs are four 32-byte runs: stored straight to HBM.
   static constexpr bool DIRECT_OUT = true;
 
@@ -1156,6 +1150,20 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
     cx<R> T[4][4];
     if constexpr (sizeof(R) == 4) {
       conj_products_f32x2(T, in[0] + i * 36, in[1] + j * 36);
+      if constexpr (PRODUCTS) {
+        if (!out) return;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+          for (int l = 0; l < 4; ++l) {
+            const int g = (k * 4 + l) * 16 + sub;
+            S *dst;
+            if constexpr (SPLIT) dst = out + (g >> 7) * sites_per_slice(ps_) * 128 + (g & 127);
+            else dst = out + g;
+            *dst = S {T[k][l].x, T[k][l].y};
+          }
+        return;
+      }
     } else {
       // Block (i, k) has the parity of k and block (j, l) that of l, so every
       // colour block loads as 16-byte vectors.
@@ -1221,13 +1229,8 @@ struct MesonAllGammaOp : OpBase<R, S, CW, 16, NST> {
       S *dst;  // 32-byte aligned
       if constexpr (SPLIT) dst = out + (a >> 3) * sites_per_slice(ps_) * 128 + (a & 7) * 16 + b0;
       else dst = out + a * 16 + b0;
-      if constexpr (ALPHA) {
-        st2(dst, mul_phase(X[h][0], alpha), mul_phase(X[h][1], alpha));
-        st2(dst + 2, mul_phase(X[h][2], alpha), mul_phase(X[h][3], alpha));
-      } else {
-        st2(dst, X[h][0], X[h][1]);
-        st2(dst + 2, X[h][2], X[h][3]);
-      }
+      st2(dst, mul_phase(X[h][0], alpha), mul_phase(X[h][1], alpha));
+      st2(dst + 2, mul_phase(X[h][2], alpha), mul_phase(X[h][3], alpha));
     }
   }
 };
