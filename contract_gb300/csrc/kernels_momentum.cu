@@ -362,7 +362,7 @@ static bool fused_disabled()
   return off;
 }
 
-static const char *const kMomFusedNames[] = {"fused.site8.xy8", "three-kernel"};
+static const char *const kMomFusedNames[] = {"fused.site8.xy8", "three-kernel", "fused.site16.xy8"};
 static const char *const kMomTcNames[] = {"tc.unit512", "tc.unit256", "tc.unit1024"};
 static const int kMomTcSteps[] = {512, 256, 1024};
 
@@ -374,7 +374,7 @@ int momentum_variants(Prec prec, int aux, const char *const **names)
   }
   if (aux == 1 && prec == Prec::C64) {
     *names = kMomFusedNames;
-    return 2;
+    return 3;
   }
   return 1;
 }
@@ -384,8 +384,8 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
 {
   if (job.volume == 0) return cudaSuccess;
   if (tensor_cores && job.prec != Prec::C64) return cudaErrorInvalidValue;
-  // job.variant (autotuner): complex64 -- 1 runs the three-kernel form; tensor
-  // cores -- the k-steps per work unit
+  // job.variant (autotuner): complex64 -- 1 runs the three-kernel form, 2 the
+  // fused kernel with 16 site warps; tensor cores -- the k-steps per work unit
   const bool fused = !tensor_cores && job.prec == Prec::C64 && momentum_fused_supported(plan) && !fused_disabled() &&
                      job.variant != 1;
   const size_t elem = job.prec == Prec::C128 ? sizeof(double2) : sizeof(float2);
@@ -402,7 +402,7 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   float2 *planes_m = reinterpret_cast<float2 *>(ws + c_bytes);   // mixed form
 
   if (fused) {
-    cudaError_t e = launch_momentum_fused(job, p.in[0], p.in[1], planes_m, plan);
+    cudaError_t e = launch_momentum_fused(job, p.in[0], p.in[1], planes_m, plan, job.variant == 2 ? 16 : 8);
     if (e != cudaSuccess) return e;
     return launch_finalize<float, true>(job, planes_m, static_cast<double2 *>(out), plan);
   }

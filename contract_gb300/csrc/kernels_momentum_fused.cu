@@ -45,7 +45,7 @@ __device__ __forceinline__ void site_products(const float2 *in0, const float2 *i
 {
   const int s = sub >> 2, i = sub & 3, j = i ^ s;
   cx<float> T[4][4];
-  conj_products_f32x2(T, in0 + i * 36, in1 + j * 36);
+  conj_products_f32x2<4>(T, in0 + i * 36, in1 + j * 36);
   if (!dst) return;
 #pragma unroll
   for (int k = 0; k < 4; ++k)
@@ -53,17 +53,47 @@ __device__ __forceinline__ void site_products(const float2 *in0, const float2 *i
     for (int l = 0; l < 4; ++l) dst[(k * 4 + l) * 16 + sub] = make_float2(T[k][l].x, T[k][l].y);
 }
 
-constexpr int kFCW = 8;                           // site warps (and transform warps)
-constexpr int kFSites = kFCW * 2;                 // sites per tile (16 threads per site)
-constexpr int kFNst = 3;                          // input ring stages
-constexpr int kFThreads = 32 * 2 * kFCW;          // 512
+// The same with a site split over 32 threads: thread sub = 8 s + 2 i + h
+// computes the 8 products of (i, j = i ^ s) with k = 2 h, 2 h + 1.
+__device__ __forceinline__ void site_products_half(const float2 *in0, const float2 *in1, int sub, float2 *dst)
+{
+  const int s = sub >> 3, i = (sub >> 1) & 3, h = sub & 1, j = i ^ s;
+  cx<float> T[2][4];
+  conj_products_f32x2<2>(T, in0 + i * 36 + h * 18, in1 + j * 36);
+  if (!dst) return;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int l = 0; l < 4; ++l) dst[((2 * h + k) * 4 + l) * 16 + s * 4 + i] = make_float2(T[k][l].x, T[k][l].y);
+}
+
+constexpr int kFTW = 8;     // transform warps (256 threads: one per product)
+constexpr int kFMaxSW = 16;  // site warps: 8 (two sites a warp) or 16 (one site a warp)
+constexpr int kFSites = 16;  // sites per tile
+constexpr int kFNst = 3;     // input ring stages
 using FL = SiteLayout<float2>;
 constexpr size_t kFStage = 2ull * kFSites * FL::SLOT;
 constexpr size_t kFOut = (size_t)kFSites * 256 * sizeof(float2);  // 32 KB per output buffer
-constexpr size_t kFStagesOff = 256;  // mbarriers: full[kFCW][kFNst], ofull[2], oempty[2]; abort flag at 248
+// mbarriers: full[SW][kFNst], ofull[2], oempty[2]; abort flag at 504
+constexpr size_t kFStagesOff = 512;
 constexpr size_t kFOutOff = kFStagesOff + kFNst * kFStage;
 constexpr size_t kFGxOff = kFOutOff + 2 * kFOut;
 constexpr size_t kFSmem = kFGxOff + (size_t)kMomMaxPx * 256 * sizeof(float2);
+static_assert((kFMaxSW * kFNst + 4) * 8 <= 504, "mbarrier block overlaps the abort flag");
+
+// Register split of the 16-site-warp shape (setmaxnreg, per warpgroup): the
+// launch gives 768 threads 80 registers each (61 440); site warps drop to 56
+// and transform warps rise to 128: 16 x 32 x 56 + 8 x 32 x 128 = 61 440.
+constexpr int kFLaunchRegs16 = 80, kFSiteRegs16 = 56, kFTransformRegs16 = 128;
+static_assert(kFMaxSW * 32 * kFSiteRegs16 + kFTW * 32 * kFTransformRegs16 <= (kFMaxSW + kFTW) * 32 * kFLaunchRegs16,
+              "register split exceeds the launch's registers");
+
+template <int SW> struct FusedShape {
+  static_assert(SW == 8 || SW == 16, "8 or 16 site warps");
+  static constexpr int THREADS = 32 * (SW + kFTW);
+  static constexpr int SPW = kFSites / SW;  // sites per site warp
+  static constexpr int TPS = 32 / SPW;      // threads per site
+};
 
 struct FusedArgs {
   const char *in[2];  // complex64 propagators, PyQUDA even/odd order
@@ -85,15 +115,16 @@ __device__ __forceinline__ long long plane_site(const MomPlan &pl, int t, int z,
   return ((((long long)par * lt + t) * lz + z) * ly + y) * half + xh;
 }
 
-template <int NG, int QC>
-__global__ void __launch_bounds__(kFThreads, 1)
+template <int SW, int NG, int QC>
+__global__ void __launch_bounds__(FusedShape<SW>::THREADS, 1)
   momentum_fused_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ MomPlan plan)
 {
+  using Shape = FusedShape<SW>;
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [kFCW][kFNst]
-  uint64_t *ofull = full + kFCW * kFNst;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);  // [SW][kFNst]
+  uint64_t *ofull = full + SW * kFNst;
   uint64_t *oempty = ofull + 2;
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 248);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 504);
   float2 *obuf = reinterpret_cast<float2 *>(smem + kFOutOff);  // [2][kFSites][256]
   __shared__ float phx[NG][kMomMaxL][2];
   __shared__ float phy[QC][kMomMaxL][2];
@@ -103,10 +134,10 @@ __global__ void __launch_bounds__(kFThreads, 1)
   const int units = lt * lz, tpp = a.tiles_per_plane, nsites = lx * ly;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kFCW * kFNst; ++s) mbar_init(&full[s], 1);
+    for (int s = 0; s < SW * kFNst; ++s) mbar_init(&full[s], 1);
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&ofull[b], kFCW);
-      mbar_init(&oempty[b], kFCW);
+      mbar_init(&ofull[b], SW);
+      mbar_init(&oempty[b], kFTW);
     }
     *abort_flag = 0;
     fence_barrier_init();
@@ -132,21 +163,23 @@ __global__ void __launch_bounds__(kFThreads, 1)
   const int my_units = blockIdx.x < units ? (units - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const int ntiles = my_units * tpp;
 
-  if (warp < kFCW) {
+  if (warp < SW) {
     // ---------------------------------------------------------- site warps
-    const int w = warp, local = lane >> 4, sub = lane & 15, site = w * 2 + local;
+    if constexpr (SW == 16) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kFSiteRegs16));
+    constexpr int SPW = Shape::SPW, TPS = Shape::TPS;
+    const int w = warp, local = lane / TPS, sub = lane % TPS, site = w * SPW + local;
     uint64_t *wfull = full + w * kFNst;
-    // Issue the copies of this warp's two sites of tile v into stage v % kFNst.
+    // Issue the copies of this warp's sites of tile v into stage v % kFNst.
     auto fetch = [&](int v) {
       const int unit = blockIdx.x + (v / tpp) * gridDim.x, k = v % tpp;
       const int t = unit / lz, z = unit - t * lz;
-      const int j0 = k * kFSites + w * 2, n = max(0, min(2, nsites - j0));
+      const int j0 = k * kFSites + w * SPW, n = max(0, min(SPW, nsites - j0));
       const int stage = v % kFNst;
       if (lane == 0) mbar_arrive_expect_tx(&wfull[stage], (uint32_t)n * 2 * FL::SITE_BYTES);
       __syncwarp();
       if (lane < 2 * n) {
         const int q = lane / n, s = lane - q * n;
-        bulk_g2s(smem + kFStagesOff + stage * kFStage + ((size_t)q * kFSites + w * 2 + s) * FL::SLOT,
+        bulk_g2s(smem + kFStagesOff + stage * kFStage + ((size_t)q * kFSites + w * SPW + s) * FL::SLOT,
                  a.in[q] + plane_site(plan, t, z, j0 + s) * FL::SITE_BYTES, FL::SITE_BYTES, &wfull[stage]);
       }
     };
@@ -176,7 +209,8 @@ __global__ void __launch_bounds__(kFThreads, 1)
       const float2 *in[2] = {reinterpret_cast<const float2 *>(sb + (size_t)site * FL::SLOT),
                              reinterpret_cast<const float2 *>(sb + ((size_t)kFSites + site) * FL::SLOT)};
       float2 *dst = site < n ? obuf + ((size_t)ob * kFSites + site) * 256 : nullptr;
-      site_products(in[0], in[1], sub, dst);
+      if constexpr (SW == 8) site_products(in[0], in[1], sub, dst);
+      else site_products_half(in[0], in[1], sub, dst);
       __threadfence_block();
       __syncwarp();
       if (lane == 0) mbar_arrive(&ofull[ob]);
@@ -185,7 +219,8 @@ __global__ void __launch_bounds__(kFThreads, 1)
   }
 
   // ------------------------------------------------------ transform warps
-  const int g = threadIdx.x - 32 * kFCW;
+  if constexpr (SW == 16) asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kFTransformRegs16));
+  const int g = threadIdx.x - 32 * SW;
   const int half = lx >> 1;
   const bool aligned = half % kFSites == 0;  // every tile lies in one half-row
   const bool zero0 = plan.gx_k[0] == 0;      // X group 0 is nx = 0: C = sum v, S = 0
@@ -275,29 +310,47 @@ __global__ void __launch_bounds__(kFThreads, 1)
   }
 }
 
-template <int NG, int QC> cudaError_t launch_fused_qc(const Job &job, const FusedArgs &a, const MomPlan &plan)
+template <int SW, int NG, int QC> cudaError_t launch_fused_qc(const Job &job, const FusedArgs &a, const MomPlan &plan)
 {
-  static int bps_cache[64] = {};
+  static int attr_set[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev >= 64 || !bps_cache[dev]) {
-    e = cudaFuncSetAttribute(momentum_fused_kernel<NG, QC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFSmem);
+  if (dev >= 64 || !attr_set[dev]) {
+    e = cudaFuncSetAttribute(momentum_fused_kernel<SW, NG, QC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kFSmem);
     if (e != cudaSuccess) return e;
-    if (dev < 64) bps_cache[dev] = 1;
+    if constexpr (SW == 16) {
+      // the register split above assumes exactly this many registers per thread at launch
+      cudaFuncAttributes fa {};
+      e = cudaFuncGetAttributes(&fa, momentum_fused_kernel<SW, NG, QC>);
+      if (e != cudaSuccess) return e;
+      if (fa.numRegs != kFLaunchRegs16) return cudaErrorInvalidConfiguration;
+    }
+    if (dev < 64) attr_set[dev] = 1;
   }
   const int units = plan.latt[3] * plan.latt[2];
   const int grid = units < job.num_sms ? units : job.num_sms;
-  momentum_fused_kernel<NG, QC><<<grid, kFThreads, kFSmem, job.stream>>>(a, plan);
+  momentum_fused_kernel<SW, NG, QC><<<grid, FusedShape<SW>::THREADS, kFSmem, job.stream>>>(a, plan);
   return cudaGetLastError();
 }
 
-template <int NG> cudaError_t launch_fused_ng(const Job &job, const FusedArgs &a, const MomPlan &plan)
+template <int SW, int NG> cudaError_t launch_fused_ng(const Job &job, const FusedArgs &a, const MomPlan &plan)
 {
-  if (plan.nq <= 4) return launch_fused_qc<NG, 4>(job, a, plan);
-  if (plan.nq <= 9) return launch_fused_qc<NG, 9>(job, a, plan);
-  if (plan.nq <= 16) return launch_fused_qc<NG, 16>(job, a, plan);
-  return launch_fused_qc<NG, kMomQChunk>(job, a, plan);
+  if (plan.nq <= 4) return launch_fused_qc<SW, NG, 4>(job, a, plan);
+  if (plan.nq <= 9) return launch_fused_qc<SW, NG, 9>(job, a, plan);
+  if (plan.nq <= 16) return launch_fused_qc<SW, NG, 16>(job, a, plan);
+  return launch_fused_qc<SW, NG, kMomQChunk>(job, a, plan);
+}
+
+template <int SW> cudaError_t launch_fused_sw(const Job &job, const FusedArgs &a, const MomPlan &plan)
+{
+  switch (plan.ngx) {
+  case 1: return launch_fused_ng<SW, 1>(job, a, plan);
+  case 2: return launch_fused_ng<SW, 2>(job, a, plan);
+  case 3: return launch_fused_ng<SW, 3>(job, a, plan);
+  default: return cudaErrorInvalidValue;
+  }
 }
 
 } // namespace
@@ -309,7 +362,7 @@ bool momentum_fused_supported(const MomPlan &plan)
 }
 
 cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *in_j, float2 *planes,
-                                  const MomPlan &plan)
+                                  const MomPlan &plan, int site_warps)
 {
   if (!momentum_fused_supported(plan)) return cudaErrorInvalidValue;
   FusedArgs a {};
@@ -318,12 +371,7 @@ cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *
   a.planes = planes;
   a.status = job.status;
   a.tiles_per_plane = (plan.latt[0] * plan.latt[1] + kFSites - 1) / kFSites;
-  switch (plan.ngx) {
-  case 1: return launch_fused_ng<1>(job, a, plan);
-  case 2: return launch_fused_ng<2>(job, a, plan);
-  case 3: return launch_fused_ng<3>(job, a, plan);
-  default: return cudaErrorInvalidValue;
-  }
+  return site_warps == 16 ? launch_fused_sw<16>(job, a, plan) : launch_fused_sw<8>(job, a, plan);
 }
 
 } // namespace cgb

@@ -53,11 +53,12 @@ cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom
 // propagators.  Supported for up to three X groups and kMomQChunk pairs.
 bool momentum_fused_supported(const MomPlan &plan);
 cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *in_j, float2 *planes,
-                                  const MomPlan &plan);
+                                  const MomPlan &plan, int site_warps = 8);
 
 // Tile-shape variants of the projection for the autotuner (Kind::Momentum).
 // aux = 2 * tensor_cores + (fused form supported):
-//   1: complex64 fused (default) or three kernels; 2, 3: tensor-core unit sizes.
+//   1: complex64 fused with 8 or 16 site warps, or three kernels;
+//   2, 3: tensor-core unit sizes.
 int momentum_variants(Prec prec, int aux, const char *const **names);
 
 // All-gamma meson correlators at the plan's momenta: out[p][t][16*16]

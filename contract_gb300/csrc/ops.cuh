@@ -1018,18 +1018,21 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
 // halves the issue slots of the products.  Colour index outermost, so only
 // one colour of each block is live; per element the FMA order is that of
 // cfma_conj, so the sums are the same to the bit.
-__device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[4][4], const float2 *xr, const float2 *yr)
+// NK consecutive colour blocks of the spin row (xr[9k..] for k < NK): the
+// half-row form serves a site split over two threads.
+template <int NK>
+__device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[NK][4], const float2 *xr, const float2 *yr)
 {
-  float2 acc[4][4];
+  float2 acc[NK][4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < NK; ++k)
 #pragma unroll
     for (int l = 0; l < 4; ++l) acc[k][l] = make_float2(0.f, 0.f);
 #pragma unroll 3  // fully unrolled, the loads of later colours run ahead and spill at 128 registers
   for (int e = 0; e < 9; ++e) {
-    float2 a[4], ar[4], b[4];
+    float2 a[NK], ar[NK], b[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < NK; ++k) {
       a[k] = xr[k * 9 + e];
       ar[k] = make_float2(a[k].y, -a[k].x);
     }
@@ -1039,14 +1042,14 @@ __device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[4][4], const 
     for (int l = 0; l < 4; ++l) {
       const float2 bx = make_float2(b[l].x, b[l].x), by = make_float2(b[l].y, b[l].y);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < NK; ++k) {
         acc[k][l] = __ffma2_rn(a[k], bx, acc[k][l]);
         acc[k][l] = __ffma2_rn(ar[k], by, acc[k][l]);
       }
     }
   }
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
+  for (int k = 0; k < NK; ++k)
 #pragma unroll
     for (int l = 0; l < 4; ++l) T[k][l] = {acc[k][l].x, acc[k][l].y};
 }

@@ -15,7 +15,7 @@ sys.path.insert(0, ROOT)
 from oracle import einsum_oracle as eo  # noqa: E402
 
 # (lattice, precision mode) pairs; the parent's cache fixes each one's variant
-CASES = [((24, 24, 16, 2), 2), ((24, 24, 16, 1), 2), ((8, 8, 8, 2), 1)]
+CASES = [((24, 24, 16, 2), 2), ((24, 24, 16, 1), 2), ((8, 8, 8, 2), 1), ((32, 4, 16, 2), 1)]
 
 
 def main():

@@ -280,7 +280,8 @@ def test_meson_momentum_many_z_groups(api):
 def test_momentum_variants_forced(tmp_path):
     """Each tile-shape variant of the momentum projection, forced through a tune
     cache: tensor-core work units of 1024 k-steps (two units per timeslice on
-    24x24x16) and 256 (five units), and the three-kernel complex64 form."""
+    24x24x16) and 256 (five units), the three-kernel complex64 form, and the
+    fused kernel with 16 site warps (on rows of 32 sites: the aligned path)."""
     import json
     import os
     import subprocess
@@ -288,7 +289,7 @@ def test_momentum_variants_forced(tmp_path):
     cache = tmp_path / "tune.txt"
     lines = []
     for latt, aux, variant, name in [((24, 24, 16, 2), 2, 2, "tc.unit1024"), ((24, 24, 16, 1), 2, 1, "tc.unit256"),
-                                     ((8, 8, 8, 2), 1, 1, "three-kernel")]:
+                                     ((8, 8, 8, 2), 1, 1, "three-kernel"), ((32, 4, 16, 2), 1, 2, "fused.site16.xy8")]:
         v = int(np.prod(latt))
         key = f"kind=7,prec=1,aux={aux},volume={v},lt={latt[3]},half={v // latt[3] // 2}"
         lines.append(f"{key}\t{variant} {name} 1.0\n")
@@ -298,11 +299,11 @@ def test_momentum_variants_forced(tmp_path):
     res = subprocess.run([sys.executable, child], env=env, capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stderr[-2000:]
     out = json.loads(res.stdout.strip().splitlines()[-1])
-    for name in ("tc.unit1024", "tc.unit256", "three-kernel"):
+    for name in ("tc.unit1024", "tc.unit256", "three-kernel", "fused.site16.xy8"):
         assert name in out["report"], out["report"]
-    tc1024, tc256, three = out["errors"]
+    tc1024, tc256, three, site16 = out["errors"]
     assert tc1024 < TOL_C64_TC and tc256 < TOL_C64_TC
-    assert three < TOL_C64_TIMESLICE
+    assert three < TOL_C64_TIMESLICE and site16 < TOL_C64_TIMESLICE
 
 
 def test_momentum_tensor_cores_two_momentum_groups(api):
