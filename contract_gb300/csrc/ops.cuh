@@ -484,7 +484,8 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
   cx<R> a1[9], a2[9];
   load9(a1, Pi + (i * 4 + b.perm2[l]) * 9);
   load9(a2, Pj + (i * 4 + b.perm2[l]) * 9);
-  cx<R> u1[NW], u2[NW], lp[2 * NW];
+  cx<R> u1[NW], u2[NW];
+  S *lps = const_cast<S *>(q) + 9 * NW + (i * 4 + l) * 2 * NW;  // loop values, parked in shared memory
 #pragma unroll
   for (int w = 0; w < NW; ++w) u1[w] = u2[w] = czero<R>();
   const bool two = cl.ng == 2;
@@ -511,7 +512,10 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
         load9(qw, q + w * 9);
         const cx<R> sq = dot9(e1, qw);
 #pragma unroll
-        for (int v = 0; v < 2; ++v) lp[v * NW + w] = mul_phase(sq, (b.ph1[0][i] + b.ph2[v][l]) & 3u);
+        for (int v = 0; v < 2; ++v) {
+          const cx<R> lv = mul_phase(sq, (b.ph1[0][i] + b.ph2[v][l]) & 3u);
+          lps[v * NW + w] = S {lv.x, lv.y};
+        }
       }
     }
     if (two) {
@@ -549,8 +553,8 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
   const uint32_t p1 = b.ph1[0][i], p2 = b.ph1[1][i];
 #pragma unroll
   for (int w = 0; w < NW; ++w) {
-    vals[0 * NW + w] = lp[0 * NW + w];                                 // IK_JL_NM
-    vals[2 * NW + w] = lp[1 * NW + w];                                 // IL_JK_NM
+    vals[0 * NW + w] = cx<R> {lps[0 * NW + w].x, lps[0 * NW + w].y};  // IK_JL_NM
+    vals[2 * NW + w] = cx<R> {lps[1 * NW + w].x, lps[1 * NW + w].y};  // IL_JK_NM
     vals[1 * NW + w] = mul_phase(u1[w], (p1 + b.ph2[0][l]) & 3u);      // IK_JM_NL
     vals[3 * NW + w] = mul_phase(u1[w], (p1 + b.ph2[1][l]) & 3u);      // IL_JM_NK
     vals[4 * NW + w] = mul_phase(u2[w], (p2 + b.ph2[0][l]) & 3u);      // IM_JK_NL
@@ -654,7 +658,7 @@ struct BaryonFusedCliffOp : OpBase<R, S, CW, TPS, NST> {
 // (fused_merged_site): fewer N loads, more live registers.
 template <class R, class S, int CW, int TPS, int NST, int NW, int MINB = 0>
 struct BaryonFusedCliffMergedOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW);
+  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW + 16 * 2 * NW);
   static constexpr bool FIELD = false;
   static constexpr int MIN_CTAS = MINB;
   static_assert(TPS == 16, "one (i, l) pair per thread");
