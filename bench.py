@@ -14,7 +14,7 @@ propagators resident in HBM; the plain complex128 form, per-call and fused, is
 measured beside it, and the per-timeslice relative error of the mixed form
 against the plain FP64 form is reported.  ``e2e`` repeats the measurement
 through the C ABI from pinned host complex128 buffers
-(contract_baryon_all_types_host: timeslice chunks copied on two copy streams,
+(contract_baryon_all_types_host: timeslice chunks copied back to back on one copy stream,
 converted to complex64 and contracted as they arrive), with every
 host->device copy, the conversion and the read-back of the correlators inside
 the timed region.
@@ -321,8 +321,9 @@ def run_ours(args, world, rank, local):
     host_out = torch.empty(out64.shape, dtype=out64.dtype).pin_memory()
 
     def e2e_step():
-        # timeslice chunks copied from the pinned host buffers on two copy
-        # streams, converted and contracted as they arrive, correlators copied back
+        # timeslice chunks copied back to back from the pinned host buffers on
+        # one copy stream, converted and contracted as they arrive, correlators
+        # copied back
         lib.contract_baryon_all_types_host(host_out.data_ptr(), *(h.data_ptr() for h in host), v, GAMMA_CG5,
                                            GAMMA_CG5, N_PROJ, proj_ptr, 1, latt_c)
 

@@ -41,17 +41,19 @@ cudaStream_t g_stream = nullptr;
 
 constexpr cgb::GammaTables kG = cgb::build_gamma_tables();
 
+constexpr int kPipeSlots = 3;  // staging slots of the host-input pipeline
+
 struct DevState {
   int num_sms = 0;
   cgb::DeviceStatus *status = nullptr;
   void *ws = nullptr;
   size_t ws_bytes = 0;
   // Host-input pipeline (contract_baryon_all_types_host): staging buffers,
-  // two copy streams and their events; created on first use.
+  // the copy stream and the slots' events; created on first use.
   void *pipe = nullptr;
   size_t pipe_bytes = 0;
-  cudaStream_t copy[2] = {nullptr, nullptr};
-  cudaEvent_t copied[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr}, start = nullptr;
+  cudaStream_t copy = nullptr;  // host-to-device copies of the host-input pipeline
+  cudaEvent_t copied[kPipeSlots] = {}, freed[kPipeSlots] = {}, start = nullptr;
 };
 DevState g_dev[64];
 
@@ -730,13 +732,13 @@ cudaError_t run_all_types(const cgb::Job &job, const OpParams<double> &p, int np
   return p.b.cl.ng <= nproj ? tuned_launch(cgb::Kind::BaryonFused, job, nproj, run) : run(job);
 }
 
-// Staging memory, copy streams and events of the host-input pipeline.
+// Staging memory, copy stream and events of the host-input pipeline.
 bool pipeline_ready(DevState *s, size_t bytes)
 {
-  if (!s->copy[0]) {
-    for (int b = 0; b < 2; ++b) {
-      if (!cuda_ok(cudaStreamCreateWithFlags(&s->copy[b], cudaStreamNonBlocking), "cudaStreamCreateWithFlags") ||
-          !cuda_ok(cudaEventCreateWithFlags(&s->copied[b], cudaEventDisableTiming), "cudaEventCreateWithFlags") ||
+  if (!s->copy) {
+    if (!cuda_ok(cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking), "cudaStreamCreateWithFlags")) return false;
+    for (int b = 0; b < kPipeSlots; ++b) {
+      if (!cuda_ok(cudaEventCreateWithFlags(&s->copied[b], cudaEventDisableTiming), "cudaEventCreateWithFlags") ||
           !cuda_ok(cudaEventCreateWithFlags(&s->freed[b], cudaEventDisableTiming), "cudaEventCreateWithFlags"))
         return false;
     }
@@ -1012,7 +1014,7 @@ void contract_baryon_all_types_host(void *correl, const void *propag_i, const vo
   const size_t conv_bytes = precision == CONTRACT_C64 ? ((chunk_sites * site_c + 255) / 256) * 256 : 0;
   const size_t out_bytes = ((size_t)6 * nproj * chunk * 16 + 255) / 256 * 256;
   const size_t slot_bytes = 3 * stage_bytes + 3 * conv_bytes + out_bytes;
-  if (!pipeline_ready(s, 2 * slot_bytes)) return;
+  if (!pipeline_ready(s, kPipeSlots * slot_bytes)) return;
 
   OpParams<double> p {};
   fill_all_types(p, nullptr, nullptr, nullptr, nullptr, 0, gamma_ij, gamma_kl, nproj, projectors);
@@ -1020,11 +1022,13 @@ void contract_baryon_all_types_host(void *correl, const void *propag_i, const vo
   DeviceWorkspace ws(s);
   // Nothing of an earlier call may still read the staging buffers.
   if (!cuda_ok(cudaEventRecord(s->start, g_stream), "cudaEventRecord")) return;
-  for (int b = 0; b < 2; ++b)
-    if (!cuda_ok(cudaStreamWaitEvent(s->copy[b], s->start, 0), "cudaStreamWaitEvent")) return;
+  if (!cuda_ok(cudaStreamWaitEvent(s->copy, s->start, 0), "cudaStreamWaitEvent")) return;
+  // One copy stream keeps the link busy with back-to-back chunks; a chunk's
+  // slot is reused kPipeSlots chunks later, long after its conversion, so the
+  // copies never wait on the contractions.
   const int nchunk = (lt + chunk - 1) / chunk;
   for (int c = 0; c < nchunk; ++c) {
-    const int b = c & 1, t0 = c * chunk, nt = std::min(chunk, lt - t0);
+    const int b = c % kPipeSlots, t0 = c * chunk, nt = std::min(chunk, lt - t0);
     char *slot = static_cast<char *>(s->pipe) + b * slot_bytes;
     char *stage[3], *conv[3];
     for (int q = 0; q < 3; ++q) {
@@ -1032,8 +1036,8 @@ void contract_baryon_all_types_host(void *correl, const void *propag_i, const vo
       conv[q] = slot + 3 * stage_bytes + q * conv_bytes;
     }
     char *out = slot + 3 * stage_bytes + 3 * conv_bytes;
-    cudaStream_t cs = s->copy[b];
-    if (c >= 2 && !cuda_ok(cudaStreamWaitEvent(cs, s->freed[b], 0), "cudaStreamWaitEvent")) return;
+    cudaStream_t cs = s->copy;
+    if (c >= kPipeSlots && !cuda_ok(cudaStreamWaitEvent(cs, s->freed[b], 0), "cudaStreamWaitEvent")) return;
     // timeslices [t0, t0 + nt) of each parity, packed as a [2][nt][half] lattice
     const size_t piece = (size_t)nt * half * site_in;
     for (int q = 0; q < 3; ++q)

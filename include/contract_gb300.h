@@ -132,7 +132,7 @@ void contract_baryon_all_types(void *correl, const void *propag_i, const void *p
 
 /* contract_baryon_all_types from HOST complex128 propagators (pinned memory
  * for full speed) into a HOST correl [6][nproj][Lt]; lattice required.
- * Timeslice chunks of the three propagators are copied on two copy streams
+ * Timeslice chunks of the three propagators are copied back to back on one copy stream
  * while earlier chunks are converted (CONTRACT_C64) and contracted on the
  * library stream, so the copies overlap the work.  Asynchronous like every
  * other call: synchronise the library stream before reading correl or
