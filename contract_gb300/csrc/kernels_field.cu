@@ -22,10 +22,12 @@ static cudaError_t seq_dispatch(const Job &job, bool loop, int role, const OpPar
 }
 
 // complex64 variants: the two-CTA shapes keep more tiles (and stores) in flight.
-static const VariantSet<float, 4> kDiquarkM = {
+static const VariantSet<float, 6> kDiquarkM = {
   {run_field<DiquarkOp<float, float2, 6, 16, 2>>, run_field<DiquarkOp<float, float2, 8, 16, 3>>,
-   run_field<DiquarkOp<float, float2, 6, 16, 2, true>>, run_field<DiquarkOp<float, float2, 8, 16, 3, true>>},
-  {"cw6.tps16.st2", "cw8.tps16.st3", "cw6.tps16.st2.direct", "cw8.tps16.st3.direct"},
+   run_field<DiquarkOp<float, float2, 6, 16, 2, true>>, run_field<DiquarkOp<float, float2, 8, 16, 3, true>>,
+   run_field<DiquarkOp<float, float2, 4, 16, 2, true>>, run_field<DiquarkOp<float, float2, 3, 16, 3, true>>},
+  {"cw6.tps16.st2", "cw8.tps16.st3", "cw6.tps16.st2.direct", "cw8.tps16.st3.direct", "cw4.tps16.st2.direct",
+   "cw3.tps16.st3.direct"},
   0};
 
 cudaError_t launch_diquark(const Job &job, const OpParams<double> &p)
@@ -39,17 +41,18 @@ cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParam
   if (job.prec == Prec::C128) return seq_dispatch<double, double2, 4, 16, 3>(job, loop, role, p);
   const OpParams<float> q = convert_params<float>(p);
   if (job.variant == 1) return seq_dispatch<float, float2, 8, 16, 3>(job, loop, role, q);
+  if (job.variant == 2) return seq_dispatch<float, float2, 3, 16, 3>(job, loop, role, q);
   return seq_dispatch<float, float2, 5, 16, 2>(job, loop, role, q);
 }
 
-static const char *const kSequentialNames[2] = {"cw5.tps16.st2", "cw8.tps16.st3"};
+static const char *const kSequentialNames[3] = {"cw5.tps16.st2", "cw8.tps16.st3", "cw3.tps16.st3"};
 
 int field_variants(Prec prec, bool sequential, const char *const **names)
 {
   if (prec == Prec::C128) return 1;
   if (!sequential) return kDiquarkM.describe(names);
   if (names) *names = kSequentialNames;
-  return 2;
+  return 3;
 }
 
 } // namespace cgb
