@@ -207,14 +207,22 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_ke
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
     cx<R> vals[NOUT];
     Op::site(ps, in, scratch, sub, vals);
-#pragma unroll
-    for (int o = 0; o < NOUT; ++o) vals[o] = group_sum<TPS>(vals[o]);
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[stage]);
     const bool valid = site < n;
-    if (sub == 0) {
+    if constexpr (kScatterSums<TPS, NOUT>) {
+      // many outputs: thread sub keeps the site sum of output sub
+      const cx<R> mine = group_reduce_scatter<TPS, NOUT>(vals, sub);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[stage]);
+      if (sub < NOUT) sv[local * NOUT + sub] = valid ? mine : czero<R>();
+    } else {
 #pragma unroll
-      for (int o = 0; o < NOUT; ++o) sv[local * NOUT + o] = valid ? vals[o] : czero<R>();
+      for (int o = 0; o < NOUT; ++o) vals[o] = group_sum<TPS>(vals[o]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[stage]);
+      if (sub == 0) {
+#pragma unroll
+        for (int o = 0; o < NOUT; ++o) sv[local * NOUT + o] = valid ? vals[o] : czero<R>();
+      }
     }
     __syncwarp();
     if (lane < NOUT) {

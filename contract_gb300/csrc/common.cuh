@@ -124,6 +124,31 @@ template <int TPS, class R> __device__ __forceinline__ cx<R> group_sum(cx<R> v)
   return v;
 }
 
+// Sum each of NOUT values over the TPS threads of a site and leave the sum of
+// value o with the thread whose sub == o (o < NOUT <= TPS), by recursive
+// halving: at the step of lane distance h the thread keeps the upper or lower
+// half of its values as (sub & h) says and receives its partner's share of
+// that half, so TPS - 1 shuffles in all instead of NOUT log2(TPS).
+template <int TPS, int NOUT> constexpr bool kScatterSums = NOUT > TPS / 2 && NOUT <= TPS;
+template <int TPS, int NOUT, class R>
+__device__ __forceinline__ cx<R> group_reduce_scatter(const cx<R> (&vals)[NOUT], int sub)
+{
+  static_assert(NOUT <= TPS && (TPS & (TPS - 1)) == 0, "one value per thread, TPS a power of two");
+  cx<R> v[TPS];
+#pragma unroll
+  for (int i = 0; i < TPS; ++i) v[i] = i < NOUT ? vals[i] : czero<R>();
+#pragma unroll
+  for (int h = TPS / 2; h > 0; h >>= 1) {
+    const bool hi = (sub & h) != 0;
+#pragma unroll
+    for (int i = 0; i < h; ++i) {
+      const cx<R> send = hi ? v[i] : v[h + i], keep = hi ? v[h + i] : v[i];
+      v[i] = cadd(keep, shfl_xor(send, h));
+    }
+  }
+  return v[0];
+}
+
 // ------------------------------------------------------------ colour maths --
 // 3x3 colour blocks are 9 consecutive complex numbers, row = sink colour.
 

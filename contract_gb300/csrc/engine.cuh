@@ -287,6 +287,31 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) scalar_kernel(c
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
     cx<R> vals[NOUT];
     Op::site(ps, in, scratch, sub, vals);
+    if constexpr (kScatterSums<TPS, NOUT>) {
+      // many outputs: thread sub keeps the site sum of output sub
+      const cx<R> mine = group_reduce_scatter<TPS, NOUT>(vals, sub);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[stage]);  // inputs consumed; only registers below
+      const bool valid = site < n;
+      if (g.per_site) {
+        if (sub < NOUT && valid)
+          static_cast<double2 *>(p.out[sub])[first + site] = make_double2(double(mine.x), double(mine.y));
+      } else {
+        if (sub < NOUT) sv[local * NOUT + sub] = valid ? mine : czero<R>();
+        __syncwarp();
+        if (lane < NOUT) {
+#pragma unroll
+          for (int s = 0; s < SPW; ++s) chunk_acc.add(sv[s * NOUT + lane]);
+          if (it.last_in_chunk()) {
+            static_cast<double2 *>(p.out[0])[((size_t)it.chunk * CW + w) * NOUT + lane] = chunk_acc.value();
+            chunk_acc.reset();
+          }
+        }
+        __syncwarp();
+      }
+      it.next(g);
+      continue;
+    }
 #pragma unroll
     for (int o = 0; o < NOUT; ++o) vals[o] = group_sum<TPS>(vals[o]);
     __syncwarp();
