@@ -426,6 +426,11 @@ void fill_clifford(cgb::CliffordSet<double> &cl, const double *const *projs, int
     for (int w = 0; w < nw; ++w) {
       cl.coef[w][k][0] = c[w][g][0];
       cl.coef[w][k][1] = c[w][g][1];
+      for (int m = 0; m < 4; ++m) {  // coef * i^ph[k][m]
+        const double pr = re[cl.ph[k][m]], pi = im[cl.ph[k][m]];
+        cl.qc[w][k][m][0] = c[w][g][0] * pr - c[w][g][1] * pi;
+        cl.qc[w][k][m][1] = c[w][g][0] * pi + c[w][g][1] * pr;
+      }
     }
   }
 }

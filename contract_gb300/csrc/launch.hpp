@@ -112,6 +112,10 @@ template <class R> OpParams<R> convert_params(const OpParams<double> &p)
     for (int w = 0; w < 2; ++w) {
       o.b.cl.coef[w][k][0] = R(p.b.cl.coef[w][k][0]);
       o.b.cl.coef[w][k][1] = R(p.b.cl.coef[w][k][1]);
+      for (int m = 0; m < 4; ++m) {
+        o.b.cl.qc[w][k][m][0] = R(p.b.cl.qc[w][k][m][0]);
+        o.b.cl.qc[w][k][m][1] = R(p.b.cl.qc[w][k][m][1]);
+      }
     }
   }
   return o;

@@ -52,6 +52,7 @@ template <class R> struct CliffordSet {
   uint8_t ph[16][4];
   uint8_t has_phase[16];
   R coef[2][16][2];
+  R qc[2][16][4][2];  // coef[w][k] * i^ph[k][m]: the coefficient of N[perm[k][m]][m] in Q_w
 };
 
 template <class R> struct BaryonSpin {
@@ -111,17 +112,23 @@ __device__ __forceinline__ void build_q(const BaryonSpin<R> &b, const S *N, S *q
 template <class R, class S, int TPS, int NW>
 __device__ __forceinline__ void build_q_cliff(const BaryonSpin<R> &b, const S *N, S *q, int sub)
 {
+  // One colour entry ad per thread, all NW projectors at once: each N value is
+  // loaded once and scaled by the precombined coefficients qc.
   const CliffordSet<R> &cl = b.cl;
-  for (int e = sub; e < 9 * NW; e += TPS) {
-    const int w = e / 9, ad = e % 9;
-    cx<R> s = czero<R>();
-    for (int k = 0; k < cl.ng; ++k) {
-      cx<R> t = czero<R>();
+  for (int ad = sub; ad < 9; ad += TPS) {
+    cx<R> s[NW];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) t = cadd(t, mul_phase(ld<R>(N + (cl.perm[k][m] * 4 + m) * 9 + ad), cl.ph[k][m]));
-      cfma(s, cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t);
+    for (int w = 0; w < NW; ++w) s[w] = czero<R>();
+    for (int k = 0; k < cl.ng; ++k) {
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const cx<R> n = ld<R>(N + (cl.perm[k][m] * 4 + m) * 9 + ad);
+#pragma unroll
+        for (int w = 0; w < NW; ++w) cfma(s[w], cx<R> {cl.qc[w][k][m][0], cl.qc[w][k][m][1]}, n);
+      }
     }
-    st(q + e, s);
+#pragma unroll
+    for (int w = 0; w < NW; ++w) st(q + w * 9 + ad, s[w]);
   }
 }
 
