@@ -495,7 +495,7 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
   S *lps = const_cast<S *>(q) + 9 * NW + (i * 4 + l) * 2 * NW;  // loop values, parked in shared memory
 #pragma unroll
   for (int w = 0; w < NW; ++w) u1[w] = u2[w] = czero<R>();
-  const bool two = cl.ng == 2;
+  const bool two = cl.ng == 2, phased = cl.has_phase[0] || cl.has_phase[1];
   cx<R> s10 = czero<R>(), s11 = czero<R>(), s20 = czero<R>(), s21 = czero<R>();
 #pragma unroll 1
   for (int mm = 0; mm < 4; ++mm) {
@@ -525,7 +525,15 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
         }
       }
     }
-    if (two) {
+    if (two && !phased) {  // e.g. (1 +- g4)/2 = (Gamma(0) +- Gamma(8))/2: no phases to apply
+      cx<R> nn[9];
+      load9(nn, N + (cl.perm[0][m] * 4 + l) * 9);
+      s10 = cadd(s10, dot9(nn, e1));
+      s20 = cadd(s20, dot9(nn, e2));
+      load9(nn, N + (cl.perm[1][m] * 4 + l) * 9);
+      s11 = cadd(s11, dot9(nn, e1));
+      s21 = cadd(s21, dot9(nn, e2));
+    } else if (two) {
       cx<R> nn[9];
       load9(nn, N + (cl.perm[0][m] * 4 + l) * 9);
       s10 = cadd(s10, mul_phase(dot9(nn, e1), cl.ph[0][m]));
