@@ -129,6 +129,28 @@ def test_fused_all_types(api, props, c_oracle):
             assert per_t_rel(got64[t, w], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
 
 
+def test_fused_all_types_phased_projectors(api, props, c_oracle):
+    """Both fused forms with (1 +- i g1 g2)/2: two gamma-basis terms whose spin
+    phases are not all +1, the path the (1 +- g4)/2 projectors skip."""
+    from contract_gb300.pycontract import gamma_matrices
+    pi, pj, pn = props
+    g12 = gamma_matrices()[3]
+    e = np.eye(4)
+    pp = np.stack([((e + 1j * g12) / 2).reshape(16), ((e - 1j * g12) / 2).reshape(16)])
+    ref = np.zeros((6, 2, LATT[3]), np.complex128)
+    ref_site = np.zeros((6, 2, pi.shape[0]), np.complex128)
+    for t in range(6):
+        for w in range(2):
+            ref_site[t, w] = c_oracle.baryon_general_two_point(pi, pj, pn, t, 5, 5, pp[w])
+            ref[t, w] = eo.timeslice_sum(ref_site[t, w], LATT)
+    got = api.baryon_all_types(cuda(pi), cuda(pj), cuda(pn), 5, 5, pp, latt=LATT).cpu().numpy()
+    assert rel_err(got, ref) < TOL_C128
+    got64 = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp, latt=LATT).cpu().numpy()
+    for t in range(6):
+        for w in range(2):
+            assert per_t_rel(got64[t, w], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
+
+
 def test_mixed_field_ops(api, props, c_oracle):
     """complex64 diquark/sequential fields: elementwise error at FP32 level."""
     import torch
