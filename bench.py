@@ -390,8 +390,8 @@ def run_ours(args, world, rank, local):
 
 
 # ------------------------------------------------------- other workloads --
-# Further BASELINE configurations, measured on request (the default run is
-# the 24^3 x 64 baryon workload above).
+# Further workloads, measured on request (the default run is the 24^3 x 64
+# baryon workload above).
 
 def _gpu_env():
     import torch
@@ -430,7 +430,7 @@ def _rel(a, b):
 
 
 def workload_momentum32(args):
-    """BASELINE config 3: all 16 x 16 meson pairs at 125 momenta on 32^3 x 64."""
+    """All 16 x 16 meson pairs at 125 momenta on 32^3 x 64."""
     torch, lib, api, dev, stream = _gpu_env()
     from contract_gb300.lattice import synthetic_propagator
     latt = (32, 32, 32, 64)
@@ -466,7 +466,7 @@ def workload_momentum32(args):
 
 
 def workload_sequential48(args):
-    """BASELINE config 4 on 48^3 x 96: the sequential source (full volume, and
+    """On 48^3 x 96: the sequential source (full volume, and
     the t_sink = 24 insertion with zeros elsewhere), then a zero-momentum
     baryon_general two-point with (1 + g4)/2; complex128 vs complex64 storage
     of the same propagator values."""
@@ -514,7 +514,7 @@ def workload_sequential48(args):
 
 
 def workload_batch(args):
-    """BASELINE config 5: 64 sources on 16^3x32, 24^3x48 and 32^3x64 lattices,
+    """64 sources on 16^3x32, 24^3x48 and 32^3x64 lattices,
     each with the 16 x 16 meson at 27 momenta and all baryon types, as one
     CUDA graph (batched baryon launch + per-source meson pipeline), complex64;
     compared with the plain per-call FP64 form on one source per lattice."""
@@ -691,7 +691,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="use the default tile shapes")
     ap.add_argument("--profile", choices=PROFILE_OPS, help="run only this op (for ncu captures)")
     ap.add_argument("--lattice", default="24,24,24,16", help="Lx,Ly,Lz,Lt for --profile")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), help="measure another BASELINE configuration")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), help="measure another workload (momentum projection, sequential source, batch)")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
