@@ -2,7 +2,7 @@
 
 Nothing in the product (``contract_gb300``) imports this package.  Only
 ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use it, and only as the checker.
+``bench.py`` use it, and only as the oracle the CUDA path is compared with.
 
 Layers, from most to least independent of the reference's own code:
 

@@ -1,7 +1,7 @@
 /*
  * Plain-C FP64 restatement of CLQCD/contract's per-site contractions.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the CPU
+ * TEST INFRASTRUCTURE ONLY: the oracle for the CUDA path and the CPU
  * baseline timed by bench.py.  Nothing in the product links or calls it.
  *
  * It restates the reference's per-site algorithm -- a loop over the 16 spin
