@@ -151,6 +151,30 @@ def test_fused_all_types_phased_projectors(api, props, c_oracle):
             assert per_t_rel(got64[t, w], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
 
 
+def test_fused_all_types_one_and_four_term_projectors(api, props, c_oracle):
+    """The fused forms' general branch: a one-term projector (g4) and the
+    polarised (1 + g4)(1 - i g1 g2)/4, four gamma-basis terms."""
+    from contract_gb300.pycontract import gamma_matrices
+    pi, pj, pn = props
+    g = gamma_matrices()
+    e = np.eye(4)
+    pol = ((e + g[8]) @ (e - 1j * g[3]) / 4).reshape(16)
+    pp = np.stack([g[8].reshape(16), pol])
+    ref = np.zeros((6, 2, LATT[3]), np.complex128)
+    ref_site = np.zeros((6, 2, pi.shape[0]), np.complex128)
+    for t in range(6):
+        for w in range(2):
+            ref_site[t, w] = c_oracle.baryon_general_two_point(pi, pj, pn, t, 5, 5, pp[w])
+            ref[t, w] = eo.timeslice_sum(ref_site[t, w], LATT)
+    for w in range(2):  # one projector per call
+        got = api.baryon_all_types(cuda(pi), cuda(pj), cuda(pn), 5, 5, pp[w:w + 1], latt=LATT).cpu().numpy()
+        assert rel_err(got[:, 0], ref[:, w]) < TOL_C128
+        got64 = api.baryon_all_types(cuda(pi, True), cuda(pj, True), cuda(pn, True), 5, 5, pp[w:w + 1],
+                                     latt=LATT).cpu().numpy()
+        for t in range(6):
+            assert per_t_rel(got64[t, 0], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
+
+
 def test_mixed_field_ops(api, props, c_oracle):
     """complex64 diquark/sequential fields: elementwise error at FP32 level."""
     import torch
