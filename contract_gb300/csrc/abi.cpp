@@ -734,7 +734,8 @@ void fill_all_types(OpParams<double> &p, const void *pi, const void *pj, const v
 cudaError_t run_all_types(const cgb::Job &job, const OpParams<double> &p, int nproj)
 {
   auto run = [&](const cgb::Job &j) { return cgb::launch_baryon_fused(j, nproj, p); };
-  return p.b.cl.ng <= nproj ? tuned_launch(cgb::Kind::BaryonFused, job, nproj, run) : run(job);
+  const int aux = nproj + (cgb::fused_same_ij(p) ? 4 : 0);
+  return p.b.cl.ng <= nproj ? tuned_launch(cgb::Kind::BaryonFused, job, aux, run) : run(job);
 }
 
 // Staging memory, copy stream and events of the host-input pipeline.
@@ -1024,6 +1025,7 @@ void contract_baryon_all_types_host(void *correl, const void *propag_i, const vo
   OpParams<double> p {};
   fill_all_types(p, nullptr, nullptr, nullptr, nullptr, 0, gamma_ij, gamma_kl, nproj, projectors);
   const void *host[3] = {propag_i, propag_j, propag_n};
+  const bool same_ij = propag_i == propag_j;
   DeviceWorkspace ws(s);
   // Nothing of an earlier call may still read the staging buffers.
   if (!cuda_ok(cudaEventRecord(s->start, g_stream), "cudaEventRecord")) return;
@@ -1043,10 +1045,12 @@ void contract_baryon_all_types_host(void *correl, const void *propag_i, const vo
     char *out = slot + 3 * stage_bytes + 3 * conv_bytes;
     cudaStream_t cs = s->copy;
     if (c >= kPipeSlots && !cuda_ok(cudaStreamWaitEvent(cs, s->freed[b], 0), "cudaStreamWaitEvent")) return;
-    // timeslices [t0, t0 + nt) of each parity, packed as a [2][nt][half] lattice
+    // timeslices [t0, t0 + nt) of each parity, packed as a [2][nt][half] lattice;
+    // P_j given as the same host buffer as P_i is copied and converted once
     const size_t piece = (size_t)nt * half * site_in;
     for (int q = 0; q < 3; ++q)
       for (int par = 0; par < 2; ++par) {
+        if (q == 1 && same_ij) continue;
         const char *src = static_cast<const char *>(host[q]) + ((size_t)par * lt + t0) * half * site_in;
         if (!cuda_ok(cudaMemcpyAsync(stage[q] + par * piece, src, piece, cudaMemcpyHostToDevice, cs),
                      "cudaMemcpyAsync"))
@@ -1062,11 +1066,13 @@ void contract_baryon_all_types_host(void *correl, const void *propag_i, const vo
     const char *in[3] = {stage[0], stage[1], stage[2]};
     if (precision == CONTRACT_C64) {
       for (int q = 0; q < 3; ++q) {
+        if (q == 1 && same_ij) continue;
         if (!cuda_ok(cgb::launch_convert(job, conv[q], stage[q], true), "contract_baryon_all_types_host")) return;
         in[q] = conv[q];
       }
       if (!cuda_ok(cudaEventRecord(s->freed[b], g_stream), "cudaEventRecord")) return;
     }
+    if (same_ij) in[1] = in[0];
     p.in[0] = in[0];
     p.in[1] = in[1];
     p.in[2] = in[2];

@@ -67,6 +67,11 @@ cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<dou
                    : run_batch<BaryonFusedCliffOp<double, double2, 4, 16, 2, 2>>(job, p, specs, n);
   }
   const OpParams<float> q = convert_params<float>(p);
+  bool same = n > 0;  // every item's P_i and P_j one field: the one-pass form
+  for (int i = 0; i < n; ++i) same = same && specs[i].in[0] == specs[i].in[1];
+  if (same)
+    return nw == 1 ? run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3, true>>(job, q, specs, n)
+                   : run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3, true>>(job, q, specs, n);
   return nw == 1 ? run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3>>(job, q, specs, n)
                  : run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3>>(job, q, specs, n);
 }

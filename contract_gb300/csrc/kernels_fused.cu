@@ -40,6 +40,21 @@ static const VariantSet<float, 8> kFusedCliff2M = {
    "merged.cw3.tps16.st2", "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
   0};
 
+// P_i and P_j the same field (one pointer, e.g. the u quark of a proton): the
+// second triangle pass equals the first, and only one is evaluated.
+static const VariantSet<float, 3> kFusedCliff1MSame = {
+  {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3, true>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 1, 4, true>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 0, true>>},
+  {"same.cw4.tps16.st2.occ3", "same.cw3.tps16.st2.occ4", "same.cw4.tps16.st2"},
+  0};
+static const VariantSet<float, 3> kFusedCliff2MSame = {
+  {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3, true>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 2, 4, true>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 0, true>>},
+  {"same.cw4.tps16.st2.occ3", "same.cw3.tps16.st2.occ4", "same.cw4.tps16.st2"},
+  0};
+
 cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &p)
 {
   const bool cliff = p.b.cl.ng <= nw;
@@ -48,13 +63,17 @@ cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &
     return nw == 1 ? run_scalar<Fused1P>(job, p) : run_scalar<Fused2P>(job, p);
   }
   const OpParams<float> q = convert_params<float>(p);
+  if (cliff && fused_same_ij(p)) return nw == 1 ? kFusedCliff1MSame.launch(job, q) : kFusedCliff2MSame.launch(job, q);
   if (cliff) return nw == 1 ? kFusedCliff1M.launch(job, q) : kFusedCliff2M.launch(job, q);
   return nw == 1 ? run_scalar<Fused1M>(job, q) : run_scalar<Fused2M>(job, q);
 }
 
-int fused_variants(Prec prec, int nw, const char *const **names)
+// aux = nw + 4 * (P_i and P_j one field)
+int fused_variants(Prec prec, int aux, const char *const **names)
 {
   if (prec == Prec::C128) return 1;
+  const int nw = aux & 3;
+  if (aux & 4) return nw == 1 ? kFusedCliff1MSame.describe(names) : kFusedCliff2MSame.describe(names);
   return nw == 1 ? kFusedCliff1M.describe(names) : kFusedCliff2M.describe(names);
 }
 

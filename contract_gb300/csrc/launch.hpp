@@ -57,6 +57,9 @@ cudaError_t launch_meson(const Job &job, const OpParams<double> &p);
 cudaError_t launch_meson_all(const Job &job, bool source, const OpParams<double> &p);
 cudaError_t launch_baryon(const Job &job, bool loop, const OpParams<double> &p);
 cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &p);
+// The fused complex64 pass takes its one-pass form when P_i and P_j are the
+// same device pointer.
+inline bool fused_same_ij(const OpParams<double> &p) { return p.in[0] == p.in[1]; }
 cudaError_t launch_diquark(const Job &job, const OpParams<double> &p);
 cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParams<double> &p);
 cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64);

@@ -482,7 +482,7 @@ __device__ __forceinline__ void fused_triangle_pass(const BaryonSpin<R> &b, cons
 // once and dotted with both a1 ^ P_j[perm1 i][m] and a2 ^ P_i[perm1 i][m].
 // The loop form is folded into the m = l wedge of the first pass as in
 // fused_triangle_pass.  vals[type * NW + w], types in contract_enum.h order.
-template <class R, class S, int NW>
+template <class R, class S, int NW, bool SAMEIJ = false>
 __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const S *Pi, const S *Pj, const S *N,
                                                   const S *q, int i, int l, cx<R> *vals)
 {
@@ -490,7 +490,7 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
   const int j = b.perm1[i];
   cx<R> a1[9], a2[9];
   load9(a1, Pi + (i * 4 + b.perm2[l]) * 9);
-  load9(a2, Pj + (i * 4 + b.perm2[l]) * 9);
+  if constexpr (!SAMEIJ) load9(a2, Pj + (i * 4 + b.perm2[l]) * 9);
   cx<R> u1[NW], u2[NW];
   S *lps = const_cast<S *>(q) + 9 * NW + (i * 4 + l) * 2 * NW;  // loop values, parked in shared memory
 #pragma unroll
@@ -507,10 +507,12 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
 #pragma unroll
       for (int k = 0; k < 9; ++k) e1[k] = czero<R>();
       wedge_acc(e1, a1, bm);
-      load9(bm, Pi + (j * 4 + m) * 9);
+      if constexpr (!SAMEIJ) {
+        load9(bm, Pi + (j * 4 + m) * 9);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) e2[k] = czero<R>();
-      wedge_acc(e2, a2, bm);
+        for (int k = 0; k < 9; ++k) e2[k] = czero<R>();
+        wedge_acc(e2, a2, bm);
+      }
     }
     if (mm == 0) {
 #pragma unroll
@@ -529,28 +531,30 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
       cx<R> nn[9];
       load9(nn, N + (cl.perm[0][m] * 4 + l) * 9);
       s10 = cadd(s10, dot9(nn, e1));
-      s20 = cadd(s20, dot9(nn, e2));
+      if constexpr (!SAMEIJ) s20 = cadd(s20, dot9(nn, e2));
       load9(nn, N + (cl.perm[1][m] * 4 + l) * 9);
       s11 = cadd(s11, dot9(nn, e1));
-      s21 = cadd(s21, dot9(nn, e2));
+      if constexpr (!SAMEIJ) s21 = cadd(s21, dot9(nn, e2));
     } else if (two) {
       cx<R> nn[9];
       load9(nn, N + (cl.perm[0][m] * 4 + l) * 9);
       s10 = cadd(s10, mul_phase(dot9(nn, e1), cl.ph[0][m]));
-      s20 = cadd(s20, mul_phase(dot9(nn, e2), cl.ph[0][m]));
+      if constexpr (!SAMEIJ) s20 = cadd(s20, mul_phase(dot9(nn, e2), cl.ph[0][m]));
       load9(nn, N + (cl.perm[1][m] * 4 + l) * 9);
       s11 = cadd(s11, mul_phase(dot9(nn, e1), cl.ph[1][m]));
-      s21 = cadd(s21, mul_phase(dot9(nn, e2), cl.ph[1][m]));
+      if constexpr (!SAMEIJ) s21 = cadd(s21, mul_phase(dot9(nn, e2), cl.ph[1][m]));
     } else {
 #pragma unroll 1
       for (int k = 0; k < cl.ng; ++k) {
         cx<R> nn[9];
         load9(nn, N + (cl.perm[k][m] * 4 + l) * 9);
-        const cx<R> t1 = mul_phase(dot9(nn, e1), cl.ph[k][m]), t2 = mul_phase(dot9(nn, e2), cl.ph[k][m]);
+        const cx<R> t1 = mul_phase(dot9(nn, e1), cl.ph[k][m]);
 #pragma unroll
-        for (int w = 0; w < NW; ++w) {
-          cfma(u1[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t1);
-          cfma(u2[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t2);
+        for (int w = 0; w < NW; ++w) cfma(u1[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t1);
+        if constexpr (!SAMEIJ) {
+          const cx<R> t2 = mul_phase(dot9(nn, e2), cl.ph[k][m]);
+#pragma unroll
+          for (int w = 0; w < NW; ++w) cfma(u2[w], cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, t2);
         }
       }
     }
@@ -561,9 +565,15 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
       const cx<R> c0 {cl.coef[w][0][0], cl.coef[w][0][1]}, c1 {cl.coef[w][1][0], cl.coef[w][1][1]};
       cfma(u1[w], c0, s10);
       cfma(u1[w], c1, s11);
-      cfma(u2[w], c0, s20);
-      cfma(u2[w], c1, s21);
+      if constexpr (!SAMEIJ) {
+        cfma(u2[w], c0, s20);
+        cfma(u2[w], c1, s21);
+      }
     }
+  }
+  if constexpr (SAMEIJ) {  // P_i and P_j are one field: both passes give the same sums
+#pragma unroll
+    for (int w = 0; w < NW; ++w) u2[w] = u1[w];
   }
   const uint32_t p1 = b.ph1[0][i], p2 = b.ph1[1][i];
 #pragma unroll
@@ -671,7 +681,7 @@ struct BaryonFusedCliffOp : OpBase<R, S, CW, TPS, NST> {
 
 // The same six types x NW projectors with both triangle passes in one m loop
 // (fused_merged_site): fewer N loads, more live registers.
-template <class R, class S, int CW, int TPS, int NST, int NW, int MINB = 0>
+template <class R, class S, int CW, int TPS, int NST, int NW, int MINB = 0, bool SAMEIJ = false>
 struct BaryonFusedCliffMergedOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW + 16 * 2 * NW);
   static constexpr bool FIELD = false;
@@ -681,7 +691,7 @@ struct BaryonFusedCliffMergedOp : OpBase<R, S, CW, TPS, NST> {
   {
     build_q_cliff<R, S, TPS, NW>(p.b, in[2], scratch, sub);
     __syncwarp();
-    fused_merged_site<R, S, NW>(p.b, in[0], in[1], in[2], scratch, sub >> 2, sub & 3, vals);
+    fused_merged_site<R, S, NW, SAMEIJ>(p.b, in[0], in[1], in[2], scratch, sub >> 2, sub & 3, vals);
   }
 };
 

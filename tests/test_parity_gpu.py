@@ -175,6 +175,50 @@ def test_fused_all_types_one_and_four_term_projectors(api, props, c_oracle):
             assert per_t_rel(got64[t, 0], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
 
 
+def test_fused_same_field_for_i_and_j(api, props, c_oracle):
+    """P_i and P_j passed as one pointer (the u quark of a proton): the complex64
+    fused pass evaluates one triangle pass instead of two; per call, in a batch
+    and from host memory it matches the two-pass result on a copy."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    pi, _, pn = props
+    pp = np.ascontiguousarray(api.projector_plus_minus())
+    a, c = cuda(pi, True), cuda(pn, True)
+    same = api.baryon_all_types(a, a, c, 5, 5, pp, latt=LATT).cpu().numpy()
+    two = api.baryon_all_types(a, a.clone(), c, 5, 5, pp, latt=LATT).cpu().numpy()
+    assert np.abs(same - two).max() <= 1e-6 * np.abs(two).max()
+    for t in range(6):
+        for w in range(2):
+            site = c_oracle.baryon_general_two_point(pi, pi, pn, t, 5, 5, pp[w])
+            assert per_t_rel(same[t, w], eo.timeslice_sum(site, LATT), site) < TOL_C64_TIMESLICE, (t, w)
+    # batched: every item with one field for P_i and P_j
+    items, outs, refs = [], [], []
+    for k, latt in enumerate(BATCH_LATTS):
+        u = cuda(eo.make_propagator(latt, 200 + k, 0.2), True)
+        d = cuda(eo.make_propagator(latt, 300 + k, 0.3), True)
+        items.append((u, u, d, latt))
+        refs.append(api.baryon_all_types(u, u, d, 5, 5, pp, latt=latt).cpu().numpy())
+        outs.append(torch.full((6, 2, latt[3]), float("nan"), dtype=torch.complex128, device="cuda"))
+    arr = _batch_items(items, outs, lib)
+    lib.contract_baryon_all_types_batch(arr, len(outs), 5, 5, 2, pp.ctypes.data, 1)
+    torch.cuda.synchronize()
+    assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+    for out, ref in zip(outs, refs):
+        assert rel_err(out.cpu().numpy(), ref) < 1e-12
+    # from host memory, P_j the same host buffer as P_i (copied once)
+    hu = torch.from_numpy(np.ascontiguousarray(pi)).pin_memory()
+    hd = torch.from_numpy(np.ascontiguousarray(pn)).pin_memory()
+    hout = torch.empty((6, 2, LATT[3]), dtype=torch.complex128).pin_memory()
+    lib.contract_baryon_all_types_host(hout.data_ptr(), hu.data_ptr(), hu.data_ptr(), hd.data_ptr(), pi.shape[0], 5, 5,
+                                       2, pp.ctypes.data, 1, (ctypes.c_int * 4)(*LATT))
+    torch.cuda.synchronize()
+    assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+    assert np.abs(hout.numpy() - same).max() <= 1e-6 * np.abs(same).max()
+    api.check_device()
+
+
 def test_mixed_field_ops(api, props, c_oracle):
     """complex64 diquark/sequential fields: elementwise error at FP32 level."""
     import torch
