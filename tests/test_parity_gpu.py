@@ -189,6 +189,13 @@ def test_fused_same_field_for_i_and_j(api, props, c_oracle):
     same = api.baryon_all_types(a, a, c, 5, 5, pp, latt=LATT).cpu().numpy()
     two = api.baryon_all_types(a, a.clone(), c, 5, 5, pp, latt=LATT).cpu().numpy()
     assert np.abs(same - two).max() <= 1e-6 * np.abs(two).max()
+    # one projector; phased gammas; a dense projector (the two-pass general form)
+    rng = np.random.default_rng(17)
+    dense = (rng.standard_normal(16) + 1j * rng.standard_normal(16)).reshape(1, 16)
+    for gij, gkl, projs in ((5, 5, pp[:1]), (13, 10, pp), (5, 5, dense)):
+        s1 = api.baryon_all_types(a, a, c, gij, gkl, projs, latt=LATT).cpu().numpy()
+        t1 = api.baryon_all_types(a, a.clone(), c, gij, gkl, projs, latt=LATT).cpu().numpy()
+        assert np.abs(s1 - t1).max() <= 1e-6 * np.abs(t1).max(), (gij, gkl, projs.shape)
     for t in range(6):
         for w in range(2):
             site = c_oracle.baryon_general_two_point(pi, pi, pn, t, 5, 5, pp[w])
