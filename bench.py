@@ -462,6 +462,15 @@ def workload_momentum32(args):
         outtc.data_ptr(), q1.data_ptr(), q2.data_ptr(), v, lat, mp, len(moms), 2), args.steps, args.warmup, lib)
     ms128 = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
         out128.data_ptr(), p1.data_ptr(), p2.data_ptr(), v, lat, mp, len(moms), 0), 2, 1, lib)
+    # one field passed twice (a pion): Hermitian site products; against the
+    # general form on a copy of the field
+    out_same, out_copy = torch.empty_like(out64), torch.empty_like(out64)
+    ms_same = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
+        out_same.data_ptr(), q1.data_ptr(), q1.data_ptr(), v, lat, mp, len(moms), 1), args.steps, args.warmup, lib)
+    q1c = q1.clone()
+    ms_copy = _time(torch, stream, lambda: lib.contract_meson_all_gamma_momentum(
+        out_copy.data_ptr(), q1.data_ptr(), q1c.data_ptr(), v, lat, mp, len(moms), 1), args.steps, args.warmup, lib)
+    a_same, a_copy = out_same.cpu().numpy(), out_copy.cpu().numpy()
     units = v * 256
     dense_flop = 8.0 * len(moms) * 256 * v  # the per-timeslice dense complex GEMM
     ref = out128.cpu().numpy()
@@ -472,7 +481,10 @@ def workload_momentum32(args):
                       "dense_gemm_equiv_tflops_mixed": dense_flop / ms64 / 1e9,
                       "dense_gemm_equiv_tflops_tensor": dense_flop / ms_tc / 1e9,
                       "accuracy_mixed_vs_plain": _rel(out64.cpu().numpy(), ref),
-                      "accuracy_tensor_vs_plain": _rel(outtc.cpu().numpy(), ref)}), flush=True)
+                      "accuracy_tensor_vs_plain": _rel(outtc.cpu().numpy(), ref),
+                      "same_field": {"ms": ms_same, "general_form_on_a_copy_ms": ms_copy,
+                                     "max_diff_rel_to_max": float(np.abs(a_same - a_copy).max()
+                                                                  / np.abs(a_copy).max())}}), flush=True)
 
 
 def workload_sequential48(args):

@@ -1176,7 +1176,8 @@ void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const
   OpParams<double> p {};
   p.in[0] = propag_i;
   p.in[1] = propag_j;
-  const int aux = tensor_cores ? 2 : (job.prec == cgb::Prec::C64 && cgb::momentum_fused_supported(plan) ? 1 : 0);
+  const bool fused = job.prec == cgb::Prec::C64 && cgb::momentum_fused_supported(plan);
+  const int aux = tensor_cores ? 2 : (fused ? 1 + (propag_i == propag_j ? 4 : 0) : 0);
   cuda_ok(tuned_launch(cgb::Kind::Momentum, job, aux,
                        [&](const cgb::Job &j) { return cgb::launch_meson_momentum(j, p, plan, correl, tensor_cores); }),
           "contract_meson_all_gamma_momentum");

@@ -368,11 +368,11 @@ static const int kMomTcSteps[] = {512, 256, 1024};
 
 int momentum_variants(Prec prec, int aux, const char *const **names)
 {
-  if (aux >= 2 && prec == Prec::C64) {
+  if ((aux & 2) && prec == Prec::C64) {
     *names = kMomTcNames;
     return 3;
   }
-  if (aux == 1 && prec == Prec::C64) {
+  if ((aux & 1) && prec == Prec::C64) {
     *names = kMomFusedNames;
     return 3;
   }

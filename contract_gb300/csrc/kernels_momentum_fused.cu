@@ -67,6 +67,65 @@ __device__ __forceinline__ void site_products_half(const float2 *in0, const floa
     for (int l = 0; l < 4; ++l) dst[((2 * h + k) * 4 + l) * 16 + s * 4 + i] = make_float2(T[k][l].x, T[k][l].y);
 }
 
+// P_i and P_j one field (S1 = S2 = S): T[j][i][l][k] = conj(T[i][j][k][l]),
+// so 136 of the 256 products are independent.  Thread sub = 4 s + i
+// (j = i ^ s) computes rows r0, r0 + 1 of the block T[X][Y], X = min(i, j),
+// Y = max(i, j), and stores each product and its conjugate transpose: r0 = 0
+// for the lower spin's thread and 2 for the higher one's.  For s = 0
+// (X = Y = i) the block is Hermitian: rows 0 and 1 give its upper triangle
+// (the lower entries of those rows are the conjugates of stored ones and are
+// not stored), and the three entries left, T[i][i][2][2], [2][3] and [3][3],
+// fall one each to the threads (s, i) with s = 1, 2, 3.  Every product is
+// stored once; a thread forms at most 9 dots instead of 16.
+__device__ __forceinline__ void same_field_extra(const float2 *in, int s, int i, float2 *dst)
+{
+  const int ea = s == 3 ? 3 : 2, eb = s == 1 ? 2 : 3;  // (2, 2), (2, 3), (3, 3) for s = 1, 2, 3
+  cx<float> E[1][1];
+  conj_products_f32x2<1, 1>(E, in + (i * 4 + ea) * 9, in + (i * 4 + eb) * 9);
+  if (!dst) return;
+  dst[(ea * 4 + eb) * 16 + i] = make_float2(E[0][0].x, E[0][0].y);
+  if (ea != eb) dst[(eb * 4 + ea) * 16 + i] = make_float2(E[0][0].x, -E[0][0].y);
+}
+
+// Stores rows k0 .. k0 + NK - 1 of T[X][Y] (and their conjugate transposes in
+// T[Y][X]) for the threads of class s, as described above.
+template <int NK>
+__device__ __forceinline__ void store_same_field(const cx<float> (&T)[NK][4], int s, int X, int Y, int k0,
+                                                 float2 *dst)
+{
+#pragma unroll
+  for (int r = 0; r < NK; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int k = k0 + r;
+      if (s == 0 && c < k) continue;  // lower triangle of the Hermitian T[i][i]
+      dst[(k * 4 + c) * 16 + 4 * s + X] = make_float2(T[r][c].x, T[r][c].y);
+      if (s != 0 || c > k) dst[(c * 4 + k) * 16 + 4 * s + Y] = make_float2(T[r][c].x, -T[r][c].y);
+    }
+}
+
+__device__ __forceinline__ void site_products_same(const float2 *in, int sub, float2 *dst)
+{
+  const int s = sub >> 2, i = sub & 3, j = i ^ s;
+  const int X = min(i, j), Y = max(i, j), k0 = i > j ? 2 : 0;
+  cx<float> T[2][4];
+  conj_products_f32x2<2>(T, in + X * 36 + k0 * 9, in + Y * 36);
+  if (s != 0) same_field_extra(in, s, i, dst);
+  if (dst) store_same_field<2>(T, s, X, Y, k0, dst);
+}
+
+// The same over 32 threads: thread sub = 8 s + 2 i + h computes row k0 + h
+// of T[X][Y]; the threads with h = 0 and s != 0 take the three entries left.
+__device__ __forceinline__ void site_products_same_half(const float2 *in, int sub, float2 *dst)
+{
+  const int s = sub >> 3, i = (sub >> 1) & 3, h = sub & 1, j = i ^ s;
+  const int X = min(i, j), Y = max(i, j), k0 = (i > j ? 2 : 0) + h;
+  cx<float> T[1][4];
+  conj_products_f32x2<1>(T, in + X * 36 + k0 * 9, in + Y * 36);
+  if (s != 0 && h == 0) same_field_extra(in, s, i, dst);
+  if (dst) store_same_field<1>(T, s, X, Y, k0, dst);
+}
+
 constexpr int kFTW = 8;     // transform warps (256 threads: one per product)
 constexpr int kFMaxSW = 16;  // site warps: 8 (two sites a warp) or 16 (one site a warp)
 constexpr int kFSites = 16;  // sites per tile
@@ -115,7 +174,7 @@ __device__ __forceinline__ long long plane_site(const MomPlan &pl, int t, int z,
   return ((((long long)par * lt + t) * lz + z) * ly + y) * half + xh;
 }
 
-template <int SW, int NG, int QC>
+template <int SW, int NG, int QC, bool SAME>
 __global__ void __launch_bounds__(FusedShape<SW>::THREADS, 1)
   momentum_fused_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ MomPlan plan)
 {
@@ -174,10 +233,10 @@ __global__ void __launch_bounds__(FusedShape<SW>::THREADS, 1)
       const int unit = blockIdx.x + (v / tpp) * gridDim.x, k = v % tpp;
       const int t = unit / lz, z = unit - t * lz;
       const int j0 = k * kFSites + w * SPW, n = max(0, min(SPW, nsites - j0));
-      const int stage = v % kFNst;
-      if (lane == 0) mbar_arrive_expect_tx(&wfull[stage], (uint32_t)n * 2 * FL::SITE_BYTES);
+      const int stage = v % kFNst, nin = SAME ? 1 : 2;  // one field: one copy per site
+      if (lane == 0) mbar_arrive_expect_tx(&wfull[stage], (uint32_t)n * nin * FL::SITE_BYTES);
       __syncwarp();
-      if (lane < 2 * n) {
+      if (lane < nin * n) {
         const int q = lane / n, s = lane - q * n;
         bulk_g2s(smem + kFStagesOff + stage * kFStage + ((size_t)q * kFSites + w * SPW + s) * FL::SLOT,
                  a.in[q] + plane_site(plan, t, z, j0 + s) * FL::SITE_BYTES, FL::SITE_BYTES, &wfull[stage]);
@@ -209,7 +268,9 @@ __global__ void __launch_bounds__(FusedShape<SW>::THREADS, 1)
       const float2 *in[2] = {reinterpret_cast<const float2 *>(sb + (size_t)site * FL::SLOT),
                              reinterpret_cast<const float2 *>(sb + ((size_t)kFSites + site) * FL::SLOT)};
       float2 *dst = site < n ? obuf + ((size_t)ob * kFSites + site) * 256 : nullptr;
-      if constexpr (SW == 8) site_products(in[0], in[1], sub, dst);
+      if constexpr (SAME && SW == 8) site_products_same(in[0], sub, dst);
+      else if constexpr (SAME) site_products_same_half(in[0], sub, dst);
+      else if constexpr (SW == 8) site_products(in[0], in[1], sub, dst);
       else site_products_half(in[0], in[1], sub, dst);
       __threadfence_block();
       __syncwarp();
@@ -310,20 +371,21 @@ __global__ void __launch_bounds__(FusedShape<SW>::THREADS, 1)
   }
 }
 
-template <int SW, int NG, int QC> cudaError_t launch_fused_qc(const Job &job, const FusedArgs &a, const MomPlan &plan)
+template <int SW, int NG, int QC, bool SAME>
+cudaError_t launch_fused_qc(const Job &job, const FusedArgs &a, const MomPlan &plan)
 {
   static int attr_set[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev >= 64 || !attr_set[dev]) {
-    e = cudaFuncSetAttribute(momentum_fused_kernel<SW, NG, QC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(momentum_fused_kernel<SW, NG, QC, SAME>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kFSmem);
     if (e != cudaSuccess) return e;
     if constexpr (SW == 16) {
       // the register split above assumes exactly this many registers per thread at launch
       cudaFuncAttributes fa {};
-      e = cudaFuncGetAttributes(&fa, momentum_fused_kernel<SW, NG, QC>);
+      e = cudaFuncGetAttributes(&fa, momentum_fused_kernel<SW, NG, QC, SAME>);
       if (e != cudaSuccess) return e;
       if (fa.numRegs != kFLaunchRegs16) return cudaErrorInvalidConfiguration;
     }
@@ -331,24 +393,25 @@ template <int SW, int NG, int QC> cudaError_t launch_fused_qc(const Job &job, co
   }
   const int units = plan.latt[3] * plan.latt[2];
   const int grid = units < job.num_sms ? units : job.num_sms;
-  momentum_fused_kernel<SW, NG, QC><<<grid, FusedShape<SW>::THREADS, kFSmem, job.stream>>>(a, plan);
+  momentum_fused_kernel<SW, NG, QC, SAME><<<grid, FusedShape<SW>::THREADS, kFSmem, job.stream>>>(a, plan);
   return cudaGetLastError();
 }
 
-template <int SW, int NG> cudaError_t launch_fused_ng(const Job &job, const FusedArgs &a, const MomPlan &plan)
+template <int SW, int NG, bool SAME>
+cudaError_t launch_fused_ng(const Job &job, const FusedArgs &a, const MomPlan &plan)
 {
-  if (plan.nq <= 4) return launch_fused_qc<SW, NG, 4>(job, a, plan);
-  if (plan.nq <= 9) return launch_fused_qc<SW, NG, 9>(job, a, plan);
-  if (plan.nq <= 16) return launch_fused_qc<SW, NG, 16>(job, a, plan);
-  return launch_fused_qc<SW, NG, kMomQChunk>(job, a, plan);
+  if (plan.nq <= 4) return launch_fused_qc<SW, NG, 4, SAME>(job, a, plan);
+  if (plan.nq <= 9) return launch_fused_qc<SW, NG, 9, SAME>(job, a, plan);
+  if (plan.nq <= 16) return launch_fused_qc<SW, NG, 16, SAME>(job, a, plan);
+  return launch_fused_qc<SW, NG, kMomQChunk, SAME>(job, a, plan);
 }
 
-template <int SW> cudaError_t launch_fused_sw(const Job &job, const FusedArgs &a, const MomPlan &plan)
+template <int SW, bool SAME> cudaError_t launch_fused_sw(const Job &job, const FusedArgs &a, const MomPlan &plan)
 {
   switch (plan.ngx) {
-  case 1: return launch_fused_ng<SW, 1>(job, a, plan);
-  case 2: return launch_fused_ng<SW, 2>(job, a, plan);
-  case 3: return launch_fused_ng<SW, 3>(job, a, plan);
+  case 1: return launch_fused_ng<SW, 1, SAME>(job, a, plan);
+  case 2: return launch_fused_ng<SW, 2, SAME>(job, a, plan);
+  case 3: return launch_fused_ng<SW, 3, SAME>(job, a, plan);
   default: return cudaErrorInvalidValue;
   }
 }
@@ -371,7 +434,9 @@ cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *
   a.planes = planes;
   a.status = job.status;
   a.tiles_per_plane = (plan.latt[0] * plan.latt[1] + kFSites - 1) / kFSites;
-  return site_warps == 16 ? launch_fused_sw<16>(job, a, plan) : launch_fused_sw<8>(job, a, plan);
+  // P_i and P_j one field: the Hermitian form of the site products
+  if (in_i == in_j) return site_warps == 16 ? launch_fused_sw<16, true>(job, a, plan) : launch_fused_sw<8, true>(job, a, plan);
+  return site_warps == 16 ? launch_fused_sw<16, false>(job, a, plan) : launch_fused_sw<8, false>(job, a, plan);
 }
 
 } // namespace cgb

@@ -56,8 +56,8 @@ cudaError_t launch_momentum_fused(const Job &job, const void *in_i, const void *
                                   const MomPlan &plan, int site_warps = 8);
 
 // Tile-shape variants of the projection for the autotuner (Kind::Momentum).
-// aux = 2 * tensor_cores + (fused form supported):
-//   1: complex64 fused with 8 or 16 site warps, or three kernels;
+// aux = 2 * tensor_cores + (fused form supported) + 4 * (P_i and P_j one field):
+//   1, 5: complex64 fused with 8 or 16 site warps, or three kernels;
 //   2, 3: tensor-core unit sizes.
 int momentum_variants(Prec prec, int aux, const char *const **names);
 

@@ -1048,27 +1048,28 @@ struct SequentialOp : OpBase<R, S, CW, TPS, NST> {
 // one colour of each block is live; per element the FMA order is that of
 // cfma_conj, so the sums are the same to the bit.
 // NK consecutive colour blocks of the spin row (xr[9k..] for k < NK): the
-// half-row form serves a site split over two threads.
-template <int NK>
-__device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[NK][4], const float2 *xr, const float2 *yr)
+// half-row form serves a site split over two threads.  NL < 4 takes the
+// first NL blocks of yr.
+template <int NK, int NL = 4>
+__device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[NK][NL], const float2 *xr, const float2 *yr)
 {
-  float2 acc[NK][4];
+  float2 acc[NK][NL];
 #pragma unroll
   for (int k = 0; k < NK; ++k)
 #pragma unroll
-    for (int l = 0; l < 4; ++l) acc[k][l] = make_float2(0.f, 0.f);
+    for (int l = 0; l < NL; ++l) acc[k][l] = make_float2(0.f, 0.f);
 #pragma unroll 3  // fully unrolled, the loads of later colours run ahead and spill at 128 registers
   for (int e = 0; e < 9; ++e) {
-    float2 a[NK], ar[NK], b[4];
+    float2 a[NK], ar[NK], b[NL];
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
       a[k] = xr[k * 9 + e];
       ar[k] = make_float2(a[k].y, -a[k].x);
     }
 #pragma unroll
-    for (int l = 0; l < 4; ++l) b[l] = yr[l * 9 + e];
+    for (int l = 0; l < NL; ++l) b[l] = yr[l * 9 + e];
 #pragma unroll
-    for (int l = 0; l < 4; ++l) {
+    for (int l = 0; l < NL; ++l) {
       const float2 bx = make_float2(b[l].x, b[l].x), by = make_float2(b[l].y, b[l].y);
 #pragma unroll
       for (int k = 0; k < NK; ++k) {
@@ -1080,7 +1081,7 @@ __device__ __forceinline__ void conj_products_f32x2(cx<float> (&T)[NK][4], const
 #pragma unroll
   for (int k = 0; k < NK; ++k)
 #pragma unroll
-    for (int l = 0; l < 4; ++l) T[k][l] = {acc[k][l].x, acc[k][l].y};
+    for (int l = 0; l < NL; ++l) T[k][l] = {acc[k][l].x, acc[k][l].y};
 }
 
 struct ClassWalsh {

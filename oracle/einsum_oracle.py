@@ -65,6 +65,19 @@ def meson_all_gamma(p1, p2):
     return np.einsum("Aji,xikjl,Bkl->ABx", g5g, t, g5g, optimize=True)
 
 
+def meson_product_l1(p1, p2, latt):
+    """Error scale for momentum-projected meson pairs: per timeslice, the
+    largest sum_x |T(x)| over the 256 spin-colour products
+    T[i][j][k][l](x) = sum_c S1[i][k][c] conj(S2[j][l][c]) that every Gamma
+    pair is a signed sum of: [1, Lt, 1].  An FP32 projection sums terms of
+    this size.  With one field in both slots the diagonal products are
+    positive at every site, so at nonzero momentum the projection cancels
+    terms of this size and its rounding is relative to it, not to |C| or to
+    sigma of the pairs."""
+    t = np.einsum("xikad,xjlad->ijklx", _as_sites(p1), np.conj(_as_sites(p2)), optimize=True).reshape(256, -1)
+    return timeslice_sum(np.abs(t), latt).real.max(axis=0)[None, :, None]
+
+
 def _baryon_subscripts(contract_type):
     _, si, sj, sn = BARYON_TYPES[int(contract_type)]
     return si, sj, sn

@@ -20,6 +20,13 @@ TOL_C64_TIMESLICE = 1e-6
 # second-order split residuals, each <= 2^-18 relative, are dropped), with
 # FP32 accumulation; the error bound is relative to max(|C_t|, sigma_t).
 TOL_C64_TC = 3e-5
+# Mixed momentum projection with one field in both propagator slots: relative
+# to max(|C|, sigma, L1), L1 the largest per-timeslice sum of |T(x)| over the
+# spin-colour products (oracle.einsum_oracle.meson_product_l1).  The diagonal
+# products are then positive at every site, and an FP32 projection to nonzero
+# momentum cancels terms of size L1; a numpy model of that projection gives
+# 0.6-1.3e-6 of L1.
+TOL_C64_COHERENT = 2e-6
 
 LATT = (4, 4, 4, 8)
 
@@ -345,6 +352,44 @@ def test_meson_momentum_fused_tiles(api, latt):
     api.check_device()
 
 
+@pytest.mark.parametrize("latt", [(6, 6, 2, 3), (10, 4, 2, 2), (4, 4, 16, 16)])
+def test_meson_momentum_same_field(api, latt):
+    """One field for both propagators (a pion): the fused complex64 kernel forms
+    136 of the 256 spin-colour products and the rest by Hermitian symmetry; it
+    matches the oracle and the general form run on a copy of the field.  The
+    error is measured against max(|C|, sigma, L1), L1 the largest per-timeslice
+    sum of |T(x)| over the spin-colour products: the diagonal products of one
+    field are positive at every site, an FP32 projection to nonzero momentum
+    cancels terms of that size (up to 15x the pairs' sigma on these lattices),
+    and its rounding reaches every pair, in the general form as much as in
+    this one.  Tolerance 2e-6 of that scale (a numpy model of the FP32
+    projection gives 0.6-1.3e-6)."""
+    import ctypes
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    pi = eo.make_propagator(latt, 71, 0.2)
+    moms = eo.momentum_list(1)
+    site = eo.meson_all_gamma(pi, pi).reshape(256, -1)
+    ref = eo.momentum_project(site, latt, moms).transpose(1, 2, 0)
+    sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real).T[None]
+    scale = np.maximum(np.maximum(np.abs(ref), sig), eo.meson_product_l1(pi, pi, latt))
+    m = np.ascontiguousarray(moms.astype(np.int32))
+    a = cuda(pi, True)
+    got = {}
+    for name, b in (("same", a), ("copy", a.clone())):
+        out = torch.full((len(moms), latt[3], 256), float("nan"), dtype=torch.complex128, device="cuda")
+        lib.contract_meson_all_gamma_momentum(out.data_ptr(), a.data_ptr(), b.data_ptr(), pi.shape[0],
+                                              (ctypes.c_int * 4)(*latt),
+                                              m.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(moms), 1)
+        got[name] = out.cpu().numpy()
+        assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+        err = (np.abs(got[name] - ref) / scale).max()
+        assert err < TOL_C64_COHERENT, (name, err)
+    assert np.abs(got["same"] - got["copy"]).max() <= 1e-6 * np.abs(got["copy"]).max()
+    api.check_device()
+
+
 def test_meson_momentum_many_z_groups(api):
     """Ten +nz/-nz groups for one (nx, ny) pair: the finalize runs two passes over
     its groups, each staging the projected products for the Gamma-pair combination."""
@@ -378,7 +423,8 @@ def test_momentum_variants_forced(tmp_path):
     """Each tile-shape variant of the momentum projection, forced through a tune
     cache: tensor-core work units of 1024 k-steps (two units per timeslice on
     24x24x16) and 256 (five units), the three-kernel complex64 form, and the
-    fused kernel with 16 site warps (on rows of 32 sites: the aligned path)."""
+    fused kernel with 16 site warps (on rows of 32 sites: the aligned path), for
+    two fields and for one field passed twice."""
     import json
     import os
     import subprocess
@@ -386,7 +432,8 @@ def test_momentum_variants_forced(tmp_path):
     cache = tmp_path / "tune.txt"
     lines = []
     for latt, aux, variant, name in [((24, 24, 16, 2), 2, 2, "tc.unit1024"), ((24, 24, 16, 1), 2, 1, "tc.unit256"),
-                                     ((8, 8, 8, 2), 1, 1, "three-kernel"), ((32, 4, 16, 2), 1, 2, "fused.site16.xy8")]:
+                                     ((8, 8, 8, 2), 1, 1, "three-kernel"), ((32, 4, 16, 2), 1, 2, "fused.site16.xy8"),
+                                     ((32, 4, 16, 3), 5, 2, "fused.site16.xy8")]:
         v = int(np.prod(latt))
         key = f"kind=7,prec=1,aux={aux},volume={v},lt={latt[3]},half={v // latt[3] // 2}"
         lines.append(f"{key}\t{variant} {name} 1.0\n")
@@ -398,9 +445,11 @@ def test_momentum_variants_forced(tmp_path):
     out = json.loads(res.stdout.strip().splitlines()[-1])
     for name in ("tc.unit1024", "tc.unit256", "three-kernel", "fused.site16.xy8"):
         assert name in out["report"], out["report"]
-    tc1024, tc256, three, site16 = out["errors"]
+    assert "aux=5" in out["report"], out["report"]
+    tc1024, tc256, three, site16, site16_same = out["errors"]
     assert tc1024 < TOL_C64_TC and tc256 < TOL_C64_TC
     assert three < TOL_C64_TIMESLICE and site16 < TOL_C64_TIMESLICE
+    assert site16_same < TOL_C64_COHERENT, site16_same
 
 
 def test_momentum_tensor_cores_two_momentum_groups(api):
