@@ -41,10 +41,13 @@ SIGNATURES = {
     "contract_last_error_message": (c_char_p, []),
     "contract_clear_error": (None, []),
     "contract_check_device": (c_int, []),
+    "contract_set_wait_limit": (None, [ctypes.c_ulonglong]),
+    "contract_test_withhold_chunk": (None, [c_int]),
     "contract_set_stream": (None, [c_void_p]),
     "contract_get_stream": (c_void_p, []),
     "contract_set_autotune": (None, [c_int]),
     "contract_autotune_report": (c_int, [c_void_p, c_size_t]),
+    "contract_variant_names": (c_int, [c_int, c_int, c_int, c_void_p, c_size_t]),
     "contract_workspace_reserve": (c_int, [c_size_t]),
     "contract_workspace_bytes": (c_size_t, [c_int_p, c_int]),
     "contract_gamma_table": (None, [c_int_p, c_int_p]),

@@ -38,6 +38,8 @@ int g_mode = -1;
 int g_err = CONTRACT_SUCCESS;
 std::string g_msg;
 cudaStream_t g_stream = nullptr;
+unsigned long long g_wait_ns = 0;  // 0: the engines' default limit
+int g_withhold_chunk = -1;         // test hook for the next call (contract_test_withhold_chunk)
 
 constexpr cgb::GammaTables kG = cgb::build_gamma_tables();
 
@@ -56,6 +58,7 @@ struct DevState {
   cudaEvent_t copied[kPipeSlots] = {}, freed[kPipeSlots] = {}, start = nullptr;
 };
 DevState g_dev[64];
+std::mutex g_dev_mu;  // guards the first-use set-up of g_dev entries
 
 int error_mode()
 {
@@ -113,6 +116,8 @@ DevState *dev_state()
     return nullptr;
   }
   DevState &s = g_dev[d];
+  // first use on a device: two host threads may get here at once
+  std::lock_guard<std::mutex> lk(g_dev_mu);
   if (s.num_sms == 0) {
     int sms = 0;
     if (!cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d), "cudaDeviceGetAttribute"))
@@ -326,6 +331,9 @@ bool make_job(cgb::Job &job, int precision, size_t volume, const int *lattice, D
   job.status = s->status;
   job.num_sms = s->num_sms;
   job.volume = (long long)volume;
+  job.wait_ns = g_wait_ns;
+  job.withhold_chunk = g_withhold_chunk;  // one call only
+  g_withhold_chunk = -1;
   if (state) *state = s;
   return true;
 }
@@ -870,6 +878,10 @@ int contract_check_device(void)
 
 void contract_set_stream(void *stream) { g_stream = static_cast<cudaStream_t>(stream); }
 
+void contract_set_wait_limit(unsigned long long ns) { g_wait_ns = ns; }
+
+void contract_test_withhold_chunk(int chunk) { g_withhold_chunk = chunk < 0 ? -1 : chunk; }
+
 void contract_set_autotune(int enable) { g_tune.enabled = enable ? 1 : 0; }
 
 int contract_autotune_report(char *buf, size_t n)
@@ -884,6 +896,22 @@ int contract_autotune_report(char *buf, size_t n)
     buf[m] = '\0';
   }
   return (int)g_tune.choice.size();
+}
+
+int contract_variant_names(int op, int precision, int aux, char *buf, size_t n)
+{
+  if (op < 0 || op > 7) return invalid("Invalid op value %d", op), 0;
+  if (!prec_ok(precision)) return 0;
+  const char *const *names = nullptr;
+  const int cnt = cgb::launch_variants(static_cast<cgb::Kind>(op), static_cast<cgb::Prec>(precision), aux, &names);
+  std::string r;
+  for (int v = 0; names && v < cnt; ++v) r += (v ? " " : "") + std::string(names[v]);
+  if (buf && n) {
+    const size_t m = r.size() < n - 1 ? r.size() : n - 1;
+    std::memcpy(buf, r.data(), m);
+    buf[m] = '\0';
+  }
+  return cnt;
 }
 
 void *contract_get_stream(void) { return g_stream; }

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_ke
       if (lane == 0) {
         *abort_flag = 1;
         report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
-        drain<NST>(full, u);
+        drain<NST>(full, u, kWaitLimitNs);
       }
       return;
     }

@@ -41,7 +41,7 @@
 
 namespace cgb {
 
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per mbarrier wait
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per mbarrier wait (the default)
 
 struct TileGeom {
   long long volume;
@@ -52,6 +52,10 @@ struct TileGeom {
   int chunks_per_seg;
   int total_chunks;
   int per_site;  // 1: per-site outputs; 0: per-chunk FP64 partial sums
+  unsigned long long wait_ns;  // wall-time limit of every mbarrier wait
+  // Test hook: the producer never copies (nor arms the barrier of) the first
+  // tile of this chunk, so its consumers' wait runs out; -1 in normal use.
+  int withhold_chunk;
 };
 
 template <int SITES> struct TileIter {
@@ -194,7 +198,7 @@ __device__ __forceinline__ void produce(const typename Op::Params &p, unsigned c
   for (int u = 0; it.valid(g); ++u) {
     const int stage = u % NST;
     if (u >= NST) {
-      const bool ok = mbar_wait_bounded(&empty[stage], ((u / NST) - 1) & 1, kWaitLimitNs);
+      const bool ok = mbar_wait_bounded(&empty[stage], ((u / NST) - 1) & 1, g.wait_ns);
       if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) {
           *abort_flag = 1;
@@ -204,6 +208,10 @@ __device__ __forceinline__ void produce(const typename Op::Params &p, unsigned c
       }
     }
     if (*abort_flag) return;
+    if (it.k == 0 && it.chunk == g.withhold_chunk) {  // test hook: this tile never arrives
+      it.next(g);
+      continue;
+    }
     long long first;
     int n;
     it.sites(g, first, n);
@@ -221,9 +229,9 @@ __device__ __forceinline__ void produce(const typename Op::Params &p, unsigned c
 
 // A consumer warp that gave up: wait (bounded) for the copies of the next
 // NST-1 tiles, which the producer may already have issued.
-template <int NST> __device__ void drain(uint64_t *full, int from)
+template <int NST> __device__ void drain(uint64_t *full, int from, unsigned long long wait_ns)
 {
-  for (int u = from; u < from + NST; ++u) mbar_wait_bounded(&full[u % NST], (u / NST) & 1, kWaitLimitNs / 8);
+  for (int u = from; u < from + NST; ++u) mbar_wait_bounded(&full[u % NST], (u / NST) & 1, wait_ns / 8);
 }
 
 // ------------------------------------------------------------ scalar ops --
@@ -272,12 +280,12 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) scalar_kernel(c
     long long first;
     int n;
     it.sites(g, first, n);
-    const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, kWaitLimitNs);
+    const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, g.wait_ns);
     if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
       if (lane == 0) {
         *abort_flag = 1;
         report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
-        drain<NST>(full, u);
+        drain<NST>(full, u, g.wait_ns);
       }
       return;
     }
@@ -388,12 +396,12 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(co
     long long first;
     int n;
     it.sites(g, first, n);
-    const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, kWaitLimitNs);
+    const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, g.wait_ns);
     if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
       if (lane == 0) {
         *abort_flag = 1;
         report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
-        drain<NST>(full, u);
+        drain<NST>(full, u, g.wait_ns);
         bulk_wait<0>();
       }
       return;

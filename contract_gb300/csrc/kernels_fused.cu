@@ -13,10 +13,15 @@ using Fused2P = BaryonFusedOp<double, double2, 4, 16, 2, 2>;
 using Fused1M = BaryonFusedOp<float, float2, 8, 16, 2, 1>;
 using Fused2M = BaryonFusedOp<float, float2, 8, 16, 2, 2>;
 
-// complex64, FP32-issue bound: consumer warps per SM vs registers per thread; the
-// merged variants run both triangle passes in one m loop (fewer N loads, more registers).
-static const VariantSet<float, 8> kFusedCliff1M = {
-  {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3>>,
+// complex64, FP32-issue bound: consumer warps per SM vs registers per thread.  The
+// shared-wedge variants form each P_i ^ P_j wedge once for both triangle passes;
+// the merged variants run both passes in one m loop with a wedge each.
+static const VariantSet<float, 12> kFusedCliff1M = {
+  {run_scalar<BaryonFusedSharedWedgeOp<float, float2, 4, 16, 2, 1, 3>>,
+   run_scalar<BaryonFusedSharedWedgeOp<float, float2, 3, 16, 2, 1, 4>>,
+   run_scalar<BaryonFusedSharedWedgeOp<float, float2, 5, 16, 2, 1, 2>>,
+   run_scalar<BaryonFusedSharedWedgeOp<float, float2, 2, 16, 3, 1, 6>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 1, 4>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 5, 16, 2, 1>>,
@@ -24,11 +29,16 @@ static const VariantSet<float, 8> kFusedCliff1M = {
    run_scalar<BaryonFusedCliffOp<float, float2, 7, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 5, 16, 2, 1>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 3, 16, 3, 1>>},
-  {"merged.cw4.tps16.st2.occ3", "merged.cw3.tps16.st2.occ4", "merged.cw4.tps16.st2", "merged.cw5.tps16.st2",
-   "merged.cw3.tps16.st2", "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
+  {"shared.cw4.tps16.st2.occ3", "shared.cw3.tps16.st2.occ4", "shared.cw5.tps16.st2.occ2",
+   "shared.cw2.tps16.st3.occ6", "merged.cw4.tps16.st2.occ3", "merged.cw3.tps16.st2.occ4", "merged.cw4.tps16.st2",
+   "merged.cw5.tps16.st2", "merged.cw3.tps16.st2", "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
   0};
-static const VariantSet<float, 8> kFusedCliff2M = {
-  {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3>>,
+static const VariantSet<float, 12> kFusedCliff2M = {
+  {run_scalar<BaryonFusedSharedWedgeOp<float, float2, 4, 16, 2, 2, 3>>,
+   run_scalar<BaryonFusedSharedWedgeOp<float, float2, 3, 16, 2, 2, 4>>,
+   run_scalar<BaryonFusedSharedWedgeOp<float, float2, 5, 16, 2, 2, 2>>,
+   run_scalar<BaryonFusedSharedWedgeOp<float, float2, 2, 16, 3, 2, 6>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 2, 4>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 5, 16, 2, 2>>,
@@ -36,8 +46,9 @@ static const VariantSet<float, 8> kFusedCliff2M = {
    run_scalar<BaryonFusedCliffOp<float, float2, 7, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 5, 16, 2, 2>>,
    run_scalar<BaryonFusedCliffOp<float, float2, 3, 16, 3, 2>>},
-  {"merged.cw4.tps16.st2.occ3", "merged.cw3.tps16.st2.occ4", "merged.cw4.tps16.st2", "merged.cw5.tps16.st2",
-   "merged.cw3.tps16.st2", "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
+  {"shared.cw4.tps16.st2.occ3", "shared.cw3.tps16.st2.occ4", "shared.cw5.tps16.st2.occ2",
+   "shared.cw2.tps16.st3.occ6", "merged.cw4.tps16.st2.occ3", "merged.cw3.tps16.st2.occ4", "merged.cw4.tps16.st2",
+   "merged.cw5.tps16.st2", "merged.cw3.tps16.st2", "cw7.tps16.st2", "cw5.tps16.st2", "cw3.tps16.st3"},
   0};
 
 // P_i and P_j the same field (one pointer, e.g. the u quark of a proton): the

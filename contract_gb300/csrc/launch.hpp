@@ -30,6 +30,8 @@ struct Job {
   long long half_slice = 0;  // sites per (parity, t) segment = Lx*Ly*Lz/2
   Workspace *ws = nullptr;
   int variant = -1;          // tile-shape variant (-1: the launcher's default)
+  unsigned long long wait_ns = 0;  // mbarrier wait limit of the site engines (0: kWaitLimitNs)
+  int withhold_chunk = -1;         // test hook of the site engines (TileGeom::withhold_chunk)
 };
 
 // Ops whose launchers offer several compiled tile shapes (consumer warps,

@@ -31,6 +31,8 @@ inline TileGeom make_geom(const Job &job, int sites, int num_sms)
   g.chunk_tiles = std::min(g.chunk_tiles, g.tiles_per_seg);
   g.chunks_per_seg = (g.tiles_per_seg + g.chunk_tiles - 1) / g.chunk_tiles;
   g.total_chunks = g.chunks_per_seg * g.num_segs;
+  g.wait_ns = job.wait_ns ? job.wait_ns : kWaitLimitNs;
+  g.withhold_chunk = job.withhold_chunk;
   return g;
 }
 

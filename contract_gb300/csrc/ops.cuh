@@ -587,6 +587,98 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
   }
 }
 
+// Both triangle passes from one set of wedges.  The wedge is symmetric
+// (X ^ Y = Y ^ X) and every gamma permutation is an involution, so the second
+// pass's wedge P_j[i][perm2 l] ^ P_i[perm1 i][m] is the first pass's wedge
+// E[i'][x][n] = P_i[i'][x] ^ P_j[perm1 i'][n] at i' = perm1 i, x = m,
+// n = perm2 l.  Thread (i, x) forms its four wedges E[i][x][n] once and
+// dots each with the N blocks of both passes:
+//   pass 1 (IK_JM_NL, IL_JM_NK; target (i, l = perm2 x), m = n):
+//     N[perm_k n][l], coefficient coef_k i^ph_k(n), output phase fixed per thread;
+//   pass 2 (IM_JK_NL, IM_JL_NK; target (perm1 i, perm2 n), m = x):
+//     N[perm_k x][perm2 n], coefficient coef_k i^ph_k(x) = qc[.][k][x], output
+//     phase i^(ph1[1][perm1 i] + ph2[v][perm2 n]) applied per n.
+// The outputs are summed over the site's 16 threads, so a thread may add
+// terms that belong to another (i, l).  The loop types use the n = l wedge
+// (the loop form's A[i][perm2 l] ^ B[perm1 i][l]) as in fused_merged_site.
+// Per site: 64 wedges + 256 dots + 32 loop dots (4 898 complex FMA with two
+// two-term projectors) instead of 128 wedges + 256 dots + 32 (7 382).
+template <class R, class S, int NW>
+__device__ __forceinline__ void fused_shared_wedge_site(const BaryonSpin<R> &b, const S *Pi, const S *Pj, const S *N,
+                                                        const S *q, int i, int x, cx<R> *vals)
+{
+  const CliffordSet<R> &cl = b.cl;
+  const int j = b.perm1[i];
+  const int l = b.perm2[x];
+  const int ng = cl.ng;  // <= NW gamma-basis terms
+  cx<R> a[9];
+  load9(a, Pi + (i * 4 + x) * 9);
+  S *lps = const_cast<S *>(q) + 9 * NW + (i * 4 + l) * 2 * NW;  // loop values, parked in shared memory
+  cx<R> s1[NW], s2[2][NW];
+#pragma unroll
+  for (int k = 0; k < NW; ++k) s1[k] = s2[0][k] = s2[1][k] = czero<R>();
+  const uint32_t p2base = b.ph1[1][j];
+#pragma unroll 1
+  for (int mm = 0; mm < 4; ++mm) {
+    const int n = (l + mm) & 3;
+    cx<R> e[9];
+    {
+      cx<R> bn[9];
+      load9(bn, Pj + (j * 4 + n) * 9);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) e[k] = czero<R>();
+      wedge_acc(e, a, bn);
+    }
+    if (mm == 0) {  // n = l: the loop form's wedge
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        cx<R> qw[9];
+        load9(qw, q + w * 9);
+        const cx<R> sq = dot9(e, qw);
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const cx<R> lv = mul_phase(sq, (b.ph1[0][i] + b.ph2[v][l]) & 3u);
+          lps[v * NW + w] = S {lv.x, lv.y};
+        }
+      }
+    }
+    const int ln = b.perm2[n];
+    const uint32_t q0 = (p2base + b.ph2[0][ln]) & 3u, q1 = (p2base + b.ph2[1][ln]) & 3u;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+      if (k < ng) {
+        cx<R> nn[9];
+        load9(nn, N + (cl.perm[k][n] * 4 + l) * 9);  // pass 1
+        s1[k] = cadd(s1[k], mul_phase(dot9(e, nn), cl.ph[k][n]));
+        load9(nn, N + (cl.perm[k][x] * 4 + ln) * 9);  // pass 2
+        const cx<R> t = dot9(e, nn);
+        s2[0][k] = cadd(s2[0][k], mul_phase(t, q0));
+        s2[1][k] = cadd(s2[1][k], mul_phase(t, q1));
+      }
+    }
+  }
+  const uint32_t p1 = b.ph1[0][i];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    cx<R> u1 = czero<R>(), u20 = czero<R>(), u21 = czero<R>();
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+      if (k < ng) {
+        cfma(u1, cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s1[k]);
+        const cx<R> c {cl.qc[w][k][x][0], cl.qc[w][k][x][1]};
+        cfma(u20, c, s2[0][k]);
+        cfma(u21, c, s2[1][k]);
+      }
+    }
+    vals[0 * NW + w] = cx<R> {lps[0 * NW + w].x, lps[0 * NW + w].y};  // IK_JL_NM
+    vals[2 * NW + w] = cx<R> {lps[1 * NW + w].x, lps[1 * NW + w].y};  // IL_JK_NM
+    vals[1 * NW + w] = mul_phase(u1, (p1 + b.ph2[0][l]) & 3u);         // IK_JM_NL
+    vals[3 * NW + w] = mul_phase(u1, (p1 + b.ph2[1][l]) & 3u);         // IL_JM_NK
+    vals[4 * NW + w] = u20;                                            // IM_JK_NL
+    vals[5 * NW + w] = u21;                                            // IM_JL_NK
+  }
+}
+
 // ------------------------------------------------------------------ ops --
 // Common compile-time configuration of an op: CW consumer warps (plus one
 // producer warp), TPS threads per site, NST ring stages.
@@ -692,6 +784,22 @@ struct BaryonFusedCliffMergedOp : OpBase<R, S, CW, TPS, NST> {
     build_q_cliff<R, S, TPS, NW>(p.b, in[2], scratch, sub);
     __syncwarp();
     fused_merged_site<R, S, NW, SAMEIJ>(p.b, in[0], in[1], in[2], scratch, sub >> 2, sub & 3, vals);
+  }
+};
+
+// The same six types x NW projectors with every wedge shared by both triangle
+// passes (fused_shared_wedge_site): a third fewer FMAs than the merged form.
+template <class R, class S, int CW, int TPS, int NST, int NW, int MINB = 0>
+struct BaryonFusedSharedWedgeOp : OpBase<R, S, CW, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW + 16 * 2 * NW);
+  static constexpr bool FIELD = false;
+  static constexpr int MIN_CTAS = MINB;
+  static_assert(TPS == 16, "one (i, x) pair per thread");
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    build_q_cliff<R, S, TPS, NW>(p.b, in[2], scratch, sub);
+    __syncwarp();
+    fused_shared_wedge_site<R, S, NW>(p.b, in[0], in[1], in[2], scratch, sub >> 2, sub & 3, vals);
   }
 };
 

@@ -66,6 +66,18 @@ void contract_clear_error(void);
  * reported by kernels, e.g. a timed-out wait) into the sticky error. */
 int contract_check_device(void);
 
+/* Wall-time limit, in nanoseconds, of every wait of the site kernels on their
+ * own copies (0 = the default, 2 s).  A wait that runs out sets the timeout
+ * bit that contract_check_device() reports; the kernel then waits (bounded)
+ * for its copies still in flight and returns, so the context stays usable. */
+void contract_set_wait_limit(unsigned long long ns);
+/* Test hook for the timeout path: in the next call only, the site kernel's
+ * producer never issues (nor announces) the copies of the first tile of work
+ * chunk `chunk`, so the consumers waiting for that tile run out of time.  The
+ * call's results are then incomplete and contract_check_device() reports
+ * CONTRACT_ERROR_DEVICE_TIMEOUT.  A negative chunk cancels it. */
+void contract_test_withhold_chunk(int chunk);
+
 /* ---------------------------------------------------------- streams ---- */
 /* All later calls (drop-in ones included) queue work on `stream`
  * (a cudaStream_t; NULL = legacy default stream, the reference's choice). */
@@ -81,6 +93,16 @@ void contract_set_autotune(int enable);
 /* Writes "key<TAB>variant<TAB>ms" lines of the current choices into buf
  * (NUL-terminated, truncated to n); returns the number of entries. */
 int contract_autotune_report(char *buf, size_t n);
+/* Names of the compiled tile-shape variants of an op, space-separated in
+ * variant order (the order a tune-cache line's variant index refers to), into
+ * buf (NUL-terminated, truncated to n); returns their number (1: nothing to
+ * tune).  op: 0 meson, 1 baryon loop form, 2 baryon triangle form, 3 all
+ * types in one pass, 4 diquark, 5 sequential, 6 meson all-source/sink,
+ * 7 meson all-gamma momentum projection; precision CONTRACT_C128 or
+ * CONTRACT_C64; aux as in the tune-cache keys (the projector count for op 3,
+ * +4 when P_i and P_j are one field; for op 7, 2 selects the tensor-core
+ * form).  Unknown op or precision: an error, and 0. */
+int contract_variant_names(int op, int precision, int aux, char *buf, size_t n);
 
 /* Reserve `bytes` of the per-device workspace used by per-timeslice
  * reductions, so that later calls (e.g. inside CUDA graph capture) do not
@@ -177,7 +199,10 @@ typedef struct {
  * launch; items is a HOST array.  Projectors must be spanned by at most
  * nproj gamma matrices (e.g. (1 +- g4)/2).  No host synchronisation: after a
  * warm-up call (and contract_workspace_reserve) the sequence can be captured
- * in a CUDA graph. */
+ * in a CUDA graph.  When EVERY item passes one pointer as both propag_i and
+ * propag_j, the launch evaluates one triangle pass per site (the second is
+ * the same values); a single item with two distinct fields sends the whole
+ * batch to the two-pass form.  Both forms give the same bits on such items. */
 void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,
                                      int nproj, const void *projectors, int precision);
 

@@ -68,6 +68,34 @@ def test_noalloc_matches_allocating_entry_point_twice(env, prec):
     assert lib.contract_check_device() == 0
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_noalloc_one_field_and_one_projector(env, prec):
+    """The forms the allocating entry point picks by its arguments, run against
+    the static scratch: one field passed as both P_i and P_j (the one-pass
+    form), and a single projector."""
+    import torch
+    lib, api, props = env
+    if prec == 1:
+        props = [api.to_c64(p) for p in props]
+    projs = np.ascontiguousarray(api.projector_plus_minus())
+    tol = TOL_C128 if prec == 0 else TOL_C64
+    cases = [([props[0], props[0], props[2]], projs), (props, np.ascontiguousarray(projs[:1])),
+             ([props[0], props[0], props[2]], np.ascontiguousarray(projs[1:]))]
+    for k, (trip, pj) in enumerate(cases):
+        ref = api.baryon_all_types(*trip, 5, 5, pj, latt=LATT)
+        torch.cuda.synchronize()
+        ref_np = ref.cpu().numpy()
+        for call in range(2):
+            out = torch.full_like(ref, float("nan"))
+            rc = _call_noalloc(lib, out, trip, pj, prec, LATT)
+            assert rc == 0, lib.contract_last_error_message()
+            torch.cuda.synchronize()
+            got = out.cpu().numpy()
+            assert np.all(np.isfinite(got)), (k, call)
+            assert np.abs(got - ref_np).max() / np.abs(ref_np).max() <= tol, (k, call)
+    assert lib.contract_check_device() == 0
+
+
 def test_noalloc_rejects_lattices_beyond_the_static_scratch(env):
     """2 x 1 x 1 x 16384: one site per half-timeslice, so 32768 partial records
     of (at least 3) consumer warps x 12 outputs x 16 bytes -- more than the
