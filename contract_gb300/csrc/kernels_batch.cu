@@ -72,8 +72,8 @@ cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<dou
   if (same)
     return nw == 1 ? run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3, true>>(job, q, specs, n)
                    : run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3, true>>(job, q, specs, n);
-  return nw == 1 ? run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3>>(job, q, specs, n)
-                 : run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3>>(job, q, specs, n);
+  return nw == 1 ? run_batch<BaryonFusedSharedWedgeOp<float, float2, 4, 16, 2, 1, 3>>(job, q, specs, n)
+                 : run_batch<BaryonFusedSharedWedgeOp<float, float2, 4, 16, 2, 2, 3>>(job, q, specs, n);
 }
 
 } // namespace cgb

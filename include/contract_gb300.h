@@ -202,7 +202,7 @@ typedef struct {
  * in a CUDA graph.  When EVERY item passes one pointer as both propag_i and
  * propag_j, the launch evaluates one triangle pass per site (the second is
  * the same values); a single item with two distinct fields sends the whole
- * batch to the two-pass form.  Both forms give the same bits on such items. */
+ * batch to the two-pass form.  The two forms agree to FP32 rounding. */
 void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,
                                      int nproj, const void *projectors, int precision);
 
