@@ -794,7 +794,7 @@ def workload_batch(args):
 WORKLOADS = {"momentum32": workload_momentum32, "sequential48": workload_sequential48, "batch": workload_batch}
 
 
-PROFILE_OPS = ("fused", "fused128", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "momentum",
+PROFILE_OPS = ("fused", "fused128", "fusedsame", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "momentum",
                "momentum128", "momentum_tc", "meson", "meson128", "meson_all",
                "diquark", "sequential", "sequential128")
 
@@ -842,6 +842,8 @@ def run_profile(args):
     def step():
         if base == "fused":
             lib.contract_baryon_all_types(out.data_ptr(), a, b_, c, v, 5, 5, 2, projs.ctypes.data, prec, latt_c)
+        elif base == "fusedsame":  # one field passed as P_i and P_j
+            lib.contract_baryon_all_types(out.data_ptr(), a, a, c, v, 5, 5, 2, projs.ctypes.data, prec, latt_c)
         elif base in ("tri", "loop"):  # baryon_two_point form: Gamma_mn = g4
             lib.contract_baryon(out.data_ptr(), a, b_, c, 1 if base == "tri" else 0, v, 5, 5, 8, None, prec, latt_c)
         elif base == "trigen":  # general projector (1 + g4)/2

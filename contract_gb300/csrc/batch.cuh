@@ -115,7 +115,7 @@ __device__ __forceinline__ void produce_batch(const BatchParams<typename Op::R> 
     }
     const int stage = u % NST;
     if (u >= NST) {
-      const bool ok = mbar_wait_bounded(&empty[stage], ((u / NST) - 1) & 1, kWaitLimitNs);
+      const bool ok = mbar_wait_bounded_backoff(&empty[stage], ((u / NST) - 1) & 1, kWaitLimitNs, kProducerSleepNs);
       if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) {
           *abort_flag = 1;

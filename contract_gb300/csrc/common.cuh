@@ -344,6 +344,22 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return false;
 }
 
+// The same for a waiter that is normally early (a producer waiting for a ring
+// stage to be released): between polls it sleeps about `sleep_ns`, so that
+// its polling does not take issue slots from the warps it waits for.
+__device__ __forceinline__ bool mbar_wait_bounded_backoff(uint64_t *bar, uint32_t parity, uint64_t limit_ns,
+                                                          unsigned sleep_ns)
+{
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer_ns();
+  for (uint32_t it = 0; it < (1u << 26); ++it) {
+    __nanosleep(sleep_ns);
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 15u) == 15u && global_timer_ns() - t0 > limit_ns) return false;
+  }
+  return false;
+}
+
 // Global -> shared bulk copy (TMA, non-tensor form).  Both addresses 16-byte
 // aligned, bytes a multiple of 16; completion is signalled on `bar`.
 __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, uint32_t bytes, uint64_t *bar)

@@ -42,6 +42,7 @@
 namespace cgb {
 
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s per mbarrier wait (the default)
+constexpr unsigned kProducerSleepNs = 128;          // producer's sleep between polls of a busy stage
 
 struct TileGeom {
   long long volume;
@@ -198,7 +199,7 @@ __device__ __forceinline__ void produce(const typename Op::Params &p, unsigned c
   for (int u = 0; it.valid(g); ++u) {
     const int stage = u % NST;
     if (u >= NST) {
-      const bool ok = mbar_wait_bounded(&empty[stage], ((u / NST) - 1) & 1, g.wait_ns);
+      const bool ok = mbar_wait_bounded_backoff(&empty[stage], ((u / NST) - 1) & 1, g.wait_ns, kProducerSleepNs);
       if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) {
           *abort_flag = 1;

@@ -1,4 +1,6 @@
 // Batched all-types baryon contractions: many sources / lattices per launch.
+#include <mutex>
+
 #include "batch.cuh"
 #include "launch_impl.cuh"
 #include "batch.hpp"
@@ -69,6 +71,21 @@ cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<dou
   const OpParams<float> q = convert_params<float>(p);
   bool same = n > 0;  // every item's P_i and P_j one field: the one-pass form
   for (int i = 0; i < n; ++i) same = same && specs[i].in[0] == specs[i].in[1];
+  // The shared-wedge forms take the Gamma_kl^T variants as a sign (every
+  // Gamma(n) is symmetric or antisymmetric); the one-field form also needs a
+  // Gamma_ij permutation without fixed points (XOR permutations: perm1[0] != 0).
+  if (same && q.b.perm1[0] != 0) {
+    static BatchSpec two[kMaxBatch];  // inputs: the field once, then P_n
+    static std::mutex mu2;
+    std::lock_guard<std::mutex> lk(mu2);
+    if (n > kMaxBatch) return cudaErrorInvalidValue;
+    for (int i = 0; i < n; ++i) {
+      two[i] = specs[i];
+      two[i].in[1] = specs[i].in[2];
+    }
+    return nw == 1 ? run_batch<BaryonFusedSharedWedgeSameOp<float, float2, 2, 2, 1, 4>>(job, q, two, n)
+                   : run_batch<BaryonFusedSharedWedgeSameOp<float, float2, 2, 2, 2, 4>>(job, q, two, n);
+  }
   if (same)
     return nw == 1 ? run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3, true>>(job, q, specs, n)
                    : run_batch<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3, true>>(job, q, specs, n);

@@ -52,19 +52,53 @@ static const VariantSet<float, 12> kFusedCliff2M = {
   0};
 
 // P_i and P_j the same field (one pointer, e.g. the u quark of a proton): the
-// second triangle pass equals the first, and only one is evaluated.
-static const VariantSet<float, 3> kFusedCliff1MSame = {
-  {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3, true>>,
+// second triangle pass equals the first, and only one is evaluated.  The
+// shared-wedge form also forms each distinct wedge once (eight threads per
+// site); it needs a Gamma_ij permutation without fixed points and takes the
+// one-pass merged form otherwise.
+template <class Op> cudaError_t run_same_field(const Job &job, OpParams<float> q)
+{
+  if (q.b.perm1[0] == 0) {  // XOR permutations: a fixed point at 0 means the identity
+    using Fallback = BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, Op::NOUT / 6, 3, true>;
+    return run_scalar<Fallback>(job, q);
+  }
+  q.in[1] = q.in[2];  // inputs: the field once, then P_n
+  return run_scalar<Op>(job, q);
+}
+
+static const VariantSet<float, 7> kFusedCliff1MSame = {
+  {run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 3, 2, 1, 3>>,
+   run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 2, 2, 1, 4>>,
+   run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 4, 2, 1, 2>>,
+   run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 5, 2, 1, 2>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3, true>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 1, 4, true>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 0, true>>},
-  {"same.cw4.tps16.st2.occ3", "same.cw3.tps16.st2.occ4", "same.cw4.tps16.st2"},
+  {"shared_same.cw3.tps8.st2.occ3", "shared_same.cw2.tps8.st2.occ4", "shared_same.cw4.tps8.st2.occ2",
+   "shared_same.cw5.tps8.st2.occ2", "same.cw4.tps16.st2.occ3", "same.cw3.tps16.st2.occ4", "same.cw4.tps16.st2"},
   0};
-static const VariantSet<float, 3> kFusedCliff2MSame = {
-  {run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3, true>>,
+static const VariantSet<float, 7> kFusedCliff2MSame = {
+  {run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 3, 2, 2, 3>>,
+   run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 2, 2, 2, 4>>,
+   run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 4, 2, 2, 2>>,
+   run_same_field<BaryonFusedSharedWedgeSameOp<float, float2, 5, 2, 2, 2>>,
+   run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3, true>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 3, 16, 2, 2, 4, true>>,
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 0, true>>},
-  {"same.cw4.tps16.st2.occ3", "same.cw3.tps16.st2.occ4", "same.cw4.tps16.st2"},
+  {"shared_same.cw3.tps8.st2.occ3", "shared_same.cw2.tps8.st2.occ4", "shared_same.cw4.tps8.st2.occ2",
+   "shared_same.cw5.tps8.st2.occ2", "same.cw4.tps16.st2.occ3", "same.cw3.tps16.st2.occ4", "same.cw4.tps16.st2"},
   0};
+
+// The shared-wedge forms derive the Gamma_kl^T variant of each type from the
+// Gamma_kl one by the phase ph2[1] - ph2[0], which is the same in every column
+// because every Gamma(n) is symmetric or antisymmetric; checked here all the same.
+static bool kl_transpose_is_sign(const OpParams<float> &q)
+{
+  const int d = (q.b.ph2[1][0] - q.b.ph2[0][0]) & 3;
+  for (int c = 1; c < 4; ++c)
+    if (((q.b.ph2[1][c] - q.b.ph2[0][c]) & 3) != d) return false;
+  return d == 0 || d == 2;
+}
 
 cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &p)
 {
@@ -74,6 +108,13 @@ cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &
     return nw == 1 ? run_scalar<Fused1P>(job, p) : run_scalar<Fused2P>(job, p);
   }
   const OpParams<float> q = convert_params<float>(p);
+  if (cliff && !kl_transpose_is_sign(q)) {  // never for DeGrand-Rossi gammas: the merged forms need no such relation
+    if (fused_same_ij(p))
+      return nw == 1 ? run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3, true>>(job, q)
+                     : run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3, true>>(job, q);
+    return nw == 1 ? run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 1, 3>>(job, q)
+                   : run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 3>>(job, q);
+  }
   if (cliff && fused_same_ij(p)) return nw == 1 ? kFusedCliff1MSame.launch(job, q) : kFusedCliff2MSame.launch(job, q);
   if (cliff) return nw == 1 ? kFusedCliff1M.launch(job, q) : kFusedCliff2M.launch(job, q);
   return nw == 1 ? run_scalar<Fused1M>(job, q) : run_scalar<Fused2M>(job, q);

@@ -597,34 +597,31 @@ __device__ __forceinline__ void fused_merged_site(const BaryonSpin<R> &b, const 
 //     N[perm_k n][l], coefficient coef_k i^ph_k(n), output phase fixed per thread;
 //   pass 2 (IM_JK_NL, IM_JL_NK; target (perm1 i, perm2 n), m = x):
 //     N[perm_k x][perm2 n], coefficient coef_k i^ph_k(x) = qc[.][k][x], output
-//     phase i^(ph1[1][perm1 i] + ph2[v][perm2 n]) applied per n.
+//     phase i^(ph1[1][perm1 i] + ph2[0][perm2 n]) applied per n.
 // The outputs are summed over the site's 16 threads, so a thread may add
 // terms that belong to another (i, l).  The loop types use the n = l wedge
 // (the loop form's A[i][perm2 l] ^ B[perm1 i][l]) as in fused_merged_site.
-// Per site: 64 wedges + 256 dots + 32 loop dots (4 898 complex FMA with two
-// two-term projectors) instead of 128 wedges + 256 dots + 32 (7 382).
-template <class R, class S, int NW>
-__device__ __forceinline__ void fused_shared_wedge_site(const BaryonSpin<R> &b, const S *Pi, const S *Pj, const S *N,
-                                                        const S *q, int i, int x, cx<R> *vals)
+// Every Gamma(n) of the DeGrand-Rossi basis is symmetric or antisymmetric, so
+// the Gamma_kl and Gamma_kl^T variants of each type differ by one sign:
+// IL_JK_NM, IL_JM_NK and IM_JL_NK are i^v1 times IK_JL_NM, IK_JM_NL and
+// IM_JK_NL, v1 = ph2[1] - ph2[0] (0 or 2, the same in every column; the
+// launcher checks it).  Per site: 64 wedges + 256 dots + 32 loop dots (4 898
+// complex FMA with two two-term projectors) instead of 128 wedges + 256 dots
+// + 32 (7 382).
+template <class R, class S, int NW, bool PHASED>
+__device__ __forceinline__ void shared_wedge_loop(const BaryonSpin<R> &b, const cx<R> (&a)[9], const S *Pjj,
+                                                  const S *Nl, const S *const (&Nx)[NW], const S *q, S *lps,
+                                                  int l, uint32_t p2base, cx<R> (&s1)[NW], cx<R> (&s2)[NW])
 {
   const CliffordSet<R> &cl = b.cl;
-  const int j = b.perm1[i];
-  const int l = b.perm2[x];
-  const int ng = cl.ng;  // <= NW gamma-basis terms
-  cx<R> a[9];
-  load9(a, Pi + (i * 4 + x) * 9);
-  S *lps = const_cast<S *>(q) + 9 * NW + (i * 4 + l) * 2 * NW;  // loop values, parked in shared memory
-  cx<R> s1[NW], s2[2][NW];
-#pragma unroll
-  for (int k = 0; k < NW; ++k) s1[k] = s2[0][k] = s2[1][k] = czero<R>();
-  const uint32_t p2base = b.ph1[1][j];
+  const int ng = cl.ng;
 #pragma unroll 1
   for (int mm = 0; mm < 4; ++mm) {
     const int n = (l + mm) & 3;
     cx<R> e[9];
     {
       cx<R> bn[9];
-      load9(bn, Pj + (j * 4 + n) * 9);
+      load9(bn, Pjj + n * 9);
 #pragma unroll
       for (int k = 0; k < 9; ++k) e[k] = czero<R>();
       wedge_acc(e, a, bn);
@@ -635,47 +632,177 @@ __device__ __forceinline__ void fused_shared_wedge_site(const BaryonSpin<R> &b, 
         cx<R> qw[9];
         load9(qw, q + w * 9);
         const cx<R> sq = dot9(e, qw);
-#pragma unroll
-        for (int v = 0; v < 2; ++v) {
-          const cx<R> lv = mul_phase(sq, (b.ph1[0][i] + b.ph2[v][l]) & 3u);
-          lps[v * NW + w] = S {lv.x, lv.y};
-        }
+        lps[w] = S {sq.x, sq.y};
       }
     }
     const int ln = b.perm2[n];
-    const uint32_t q0 = (p2base + b.ph2[0][ln]) & 3u, q1 = (p2base + b.ph2[1][ln]) & 3u;
+    const uint32_t q0 = (p2base + b.ph2[0][ln]) & 3u;
 #pragma unroll
     for (int k = 0; k < NW; ++k) {
       if (k < ng) {
         cx<R> nn[9];
-        load9(nn, N + (cl.perm[k][n] * 4 + l) * 9);  // pass 1
-        s1[k] = cadd(s1[k], mul_phase(dot9(e, nn), cl.ph[k][n]));
-        load9(nn, N + (cl.perm[k][x] * 4 + ln) * 9);  // pass 2
-        const cx<R> t = dot9(e, nn);
-        s2[0][k] = cadd(s2[0][k], mul_phase(t, q0));
-        s2[1][k] = cadd(s2[1][k], mul_phase(t, q1));
+        load9(nn, Nl + cl.perm[k][n] * 36);  // pass 1
+        const cx<R> d = dot9(e, nn);
+        s1[k] = cadd(s1[k], PHASED ? mul_phase(d, cl.ph[k][n]) : d);
+        load9(nn, Nx[k] + ln * 9);  // pass 2
+        s2[k] = cadd(s2[k], mul_phase(dot9(e, nn), q0));
       }
     }
   }
-  const uint32_t p1 = b.ph1[0][i];
+}
+
+template <class R, class S, int NW>
+__device__ __forceinline__ void fused_shared_wedge_site(const BaryonSpin<R> &b, const S *Pi, const S *Pj, const S *N,
+                                                        const S *q, int i, int x, cx<R> *vals)
+{
+  const CliffordSet<R> &cl = b.cl;
+  const int j = b.perm1[i];
+  const int l = b.perm2[x];
+  const int ng = cl.ng;  // <= NW gamma-basis terms
+  cx<R> a[9];
+  load9(a, Pi + (i * 4 + x) * 9);
+  S *lps = const_cast<S *>(q) + 9 * NW + (i * 4 + x) * NW;  // loop values, parked in shared memory
+  const S *Nx[NW];
+#pragma unroll
+  for (int k = 0; k < NW; ++k) Nx[k] = N + (k < ng ? cl.perm[k][x] : 0) * 36;
+  cx<R> s1[NW], s2[NW];
+#pragma unroll
+  for (int k = 0; k < NW; ++k) s1[k] = s2[k] = czero<R>();
+  const uint32_t p2base = b.ph1[1][j];
+  if (cl.has_phase[0] || cl.has_phase[1])
+    shared_wedge_loop<R, S, NW, true>(b, a, Pj + j * 36, N + l * 9, Nx, q, lps, l, p2base, s1, s2);
+  else
+    shared_wedge_loop<R, S, NW, false>(b, a, Pj + j * 36, N + l * 9, Nx, q, lps, l, p2base, s1, s2);
+  const uint32_t p1 = (b.ph1[0][i] + b.ph2[0][l]) & 3u, v1 = (b.ph2[1][0] - b.ph2[0][0]) & 3u;
 #pragma unroll
   for (int w = 0; w < NW; ++w) {
-    cx<R> u1 = czero<R>(), u20 = czero<R>(), u21 = czero<R>();
+    cx<R> u1 = czero<R>(), u2 = czero<R>();
 #pragma unroll
     for (int k = 0; k < NW; ++k) {
       if (k < ng) {
         cfma(u1, cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s1[k]);
-        const cx<R> c {cl.qc[w][k][x][0], cl.qc[w][k][x][1]};
-        cfma(u20, c, s2[0][k]);
-        cfma(u21, c, s2[1][k]);
+        cfma(u2, cx<R> {cl.qc[w][k][x][0], cl.qc[w][k][x][1]}, s2[k]);
       }
     }
-    vals[0 * NW + w] = cx<R> {lps[0 * NW + w].x, lps[0 * NW + w].y};  // IK_JL_NM
-    vals[2 * NW + w] = cx<R> {lps[1 * NW + w].x, lps[1 * NW + w].y};  // IL_JK_NM
-    vals[1 * NW + w] = mul_phase(u1, (p1 + b.ph2[0][l]) & 3u);         // IK_JM_NL
-    vals[3 * NW + w] = mul_phase(u1, (p1 + b.ph2[1][l]) & 3u);         // IL_JM_NK
-    vals[4 * NW + w] = u20;                                            // IM_JK_NL
-    vals[5 * NW + w] = u21;                                            // IM_JL_NK
+    const cx<R> lv = mul_phase(cx<R> {lps[w].x, lps[w].y}, p1);
+    const cx<R> t1 = mul_phase(u1, p1);
+    vals[0 * NW + w] = lv;                  // IK_JL_NM
+    vals[2 * NW + w] = mul_phase(lv, v1);   // IL_JK_NM
+    vals[1 * NW + w] = t1;                  // IK_JM_NL
+    vals[3 * NW + w] = mul_phase(t1, v1);   // IL_JM_NK
+    vals[4 * NW + w] = u2;                  // IM_JK_NL
+    vals[5 * NW + w] = mul_phase(u2, v1);   // IM_JL_NK
+  }
+}
+
+// One field P for P_i and P_j (the proton's two u quarks), with perm1 free of
+// fixed points (Gamma_ij = C g5 and most others): the wedge E[i][x][n] =
+// P[i][x] ^ P[perm1 i][n] is also the wedge of slot (perm1 i, n, x), and with
+// one field the second triangle pass equals the first.  So eight threads per
+// site, thread (i, x) with i < perm1 i, form the 32 distinct wedges once and
+// each wedge serves two slots:
+//   own slot (i, x, n):           target (i, l = perm2 x), m = n  -- as pass 1 above
+//   partner slot (perm1 i, n, x): target (perm1 i, perm2 n), m = x -- the N blocks
+//                                 and coefficients of pass 2 above
+// Both targets feed all four triangle types (IK_JM_NL with the Gamma_ij phase
+// row of P_i first, IM_JK_NL with the transposed row; the Gamma_kl^T variants
+// by the sign i^v1 as above); the n = l wedge gives the loop values of both
+// targets.  Per site: 32 wedges + 128 dots + 16 loop dots (2 592 complex FMA
+// with two two-term projectors) instead of the one-pass form's 64 + 128 + 32
+// (3 744).
+template <class R, class S, int NW, bool PHASED>
+__device__ __forceinline__ void shared_wedge_same_loop(const BaryonSpin<R> &b, const cx<R> (&a)[9], const S *Pjj,
+                                                       const S *Nl, const S *const (&Nx)[NW], const S *q, S *lps,
+                                                       int l, uint32_t lph, cx<R> (&s1)[NW], cx<R> (&s2)[NW])
+{
+  const CliffordSet<R> &cl = b.cl;
+  const int ng = cl.ng;
+#pragma unroll 1
+  for (int mm = 0; mm < 4; ++mm) {
+    const int n = (l + mm) & 3;
+    cx<R> e[9];
+    {
+      cx<R> bn[9];
+      load9(bn, Pjj + n * 9);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) e[k] = czero<R>();
+      wedge_acc(e, a, bn);
+    }
+    if (mm == 0) {  // n = l: the loop wedge of (i, l) and of the partner target (j, x)
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        cx<R> qw[9];
+        load9(qw, q + w * 9);
+        const cx<R> sq = dot9(e, qw);
+        const cx<R> lv = cadd(sq, mul_phase(sq, lph));  // own phase factored out: 1 + i^(partner - own)
+        lps[w] = S {lv.x, lv.y};
+      }
+    }
+    const int ln = b.perm2[n];
+    const uint32_t q0 = b.ph2[0][ln];
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+      if (k < ng) {
+        cx<R> nn[9];
+        load9(nn, Nl + cl.perm[k][n] * 36);  // own slot
+        const cx<R> d = dot9(e, nn);
+        s1[k] = cadd(s1[k], PHASED ? mul_phase(d, cl.ph[k][n]) : d);
+        load9(nn, Nx[k] + ln * 9);  // partner slot
+        s2[k] = cadd(s2[k], mul_phase(dot9(e, nn), q0));
+      }
+    }
+  }
+}
+
+template <class R, class S, int NW>
+__device__ __forceinline__ void fused_shared_wedge_same_site(const BaryonSpin<R> &b, const S *P, const S *N,
+                                                             const S *q, int sub, cx<R> *vals)
+{
+  const CliffordSet<R> &cl = b.cl;
+  const int i = (sub >> 2) == 0 ? 0 : (b.perm1[0] == 1 ? 2 : 1);  // the two rows with i < perm1 i
+  const int x = sub & 3;
+  const int j = b.perm1[i];
+  const int l = b.perm2[x];
+  const int ng = cl.ng;
+  cx<R> a[9];
+  load9(a, P + (i * 4 + x) * 9);
+  S *lps = const_cast<S *>(q) + 9 * NW + sub * NW;  // loop values, parked in shared memory
+  const S *Nx[NW];
+#pragma unroll
+  for (int k = 0; k < NW; ++k) Nx[k] = N + (k < ng ? cl.perm[k][x] : 0) * 36;
+  cx<R> s1[NW], s2[NW];
+#pragma unroll
+  for (int k = 0; k < NW; ++k) s1[k] = s2[k] = czero<R>();
+  const uint32_t own = (b.ph1[0][i] + b.ph2[0][l]) & 3u;   // IK_JM_NL / loop phase of target (i, l)
+  const uint32_t part = (b.ph1[0][j] + b.ph2[0][x]) & 3u;  // loop phase of the partner target (j, x)
+  if (cl.has_phase[0] || cl.has_phase[1])
+    shared_wedge_same_loop<R, S, NW, true>(b, a, P + j * 36, N + l * 9, Nx, q, lps, l, (part - own) & 3u, s1, s2);
+  else
+    shared_wedge_same_loop<R, S, NW, false>(b, a, P + j * 36, N + l * 9, Nx, q, lps, l, (part - own) & 3u, s1, s2);
+  // the IM_* group takes the transposed Gamma_ij phase row: a fixed offset per row
+  const uint32_t di = (b.ph1[1][i] - b.ph1[0][i]) & 3u, dj = (b.ph1[1][j] - b.ph1[0][j]) & 3u;
+  const uint32_t v1 = (b.ph2[1][0] - b.ph2[0][0]) & 3u;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    cx<R> u1 = czero<R>(), u2 = czero<R>();
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+      if (k < ng) {
+        cfma(u1, cx<R> {cl.coef[w][k][0], cl.coef[w][k][1]}, s1[k]);
+        cfma(u2, cx<R> {cl.qc[w][k][x][0], cl.qc[w][k][x][1]}, s2[k]);
+      }
+    }
+    const cx<R> o1 = mul_phase(u1, own);   // target (i, l)
+    const cx<R> o2 = mul_phase(u2, b.ph1[0][j]);  // target (j, perm2 n): its column phase is already in s2
+    const cx<R> lv = mul_phase(cx<R> {lps[w].x, lps[w].y}, own);
+    const cx<R> t1 = cadd(o1, o2);
+    const cx<R> t2 = cadd(mul_phase(o1, di), mul_phase(o2, dj));
+    vals[0 * NW + w] = lv;                  // IK_JL_NM
+    vals[2 * NW + w] = mul_phase(lv, v1);   // IL_JK_NM
+    vals[1 * NW + w] = t1;                  // IK_JM_NL
+    vals[3 * NW + w] = mul_phase(t1, v1);   // IL_JM_NK
+    vals[4 * NW + w] = t2;                  // IM_JK_NL
+    vals[5 * NW + w] = mul_phase(t2, v1);   // IM_JL_NK
   }
 }
 
@@ -791,7 +918,7 @@ struct BaryonFusedCliffMergedOp : OpBase<R, S, CW, TPS, NST> {
 // passes (fused_shared_wedge_site): a third fewer FMAs than the merged form.
 template <class R, class S, int CW, int TPS, int NST, int NW, int MINB = 0>
 struct BaryonFusedSharedWedgeOp : OpBase<R, S, CW, TPS, NST> {
-  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW + 16 * 2 * NW);
+  static constexpr int NIN = 3, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW + 16 * NW);
   static constexpr bool FIELD = false;
   static constexpr int MIN_CTAS = MINB;
   static_assert(TPS == 16, "one (i, x) pair per thread");
@@ -800,6 +927,22 @@ struct BaryonFusedSharedWedgeOp : OpBase<R, S, CW, TPS, NST> {
     build_q_cliff<R, S, TPS, NW>(p.b, in[2], scratch, sub);
     __syncwarp();
     fused_shared_wedge_site<R, S, NW>(p.b, in[0], in[1], in[2], scratch, sub >> 2, sub & 3, vals);
+  }
+};
+
+// One field for P_i and P_j and perm1 without fixed points: eight threads per
+// site, each wedge serving two slots (fused_shared_wedge_same_site).  Two
+// inputs, in[0] = P and in[1] = P_n: the field is staged once per site.
+template <class R, class S, int CW, int NST, int NW, int MINB = 0>
+struct BaryonFusedSharedWedgeSameOp : OpBase<R, S, CW, 8, NST> {
+  static constexpr int NIN = 2, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW + 8 * NW);
+  static constexpr bool FIELD = false;
+  static constexpr int MIN_CTAS = MINB;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    build_q_cliff<R, S, 8, NW>(p.b, in[1], scratch, sub);
+    __syncwarp();
+    fused_shared_wedge_same_site<R, S, NW>(p.b, in[0], in[1], scratch, sub, vals);
   }
 };
 

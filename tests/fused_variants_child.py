@@ -22,20 +22,24 @@ def main():
     from contract_gb300 import _lib, api
     lib = _lib.lib()
     lib.contract_set_error_mode(1)
-    cases = json.loads(sys.argv[1])  # [[latt, nproj], ...]
+    cases = json.loads(sys.argv[1])  # [[latt, nproj, one field for P_i and P_j], ...]
     oracle = L.c_oracle()
     pp = api.projector_plus_minus()
     g4 = np.asarray(eo.GAMMA[8]).reshape(1, 16)
     errs = []
-    for k, (latt, nproj) in enumerate(cases):
+    for k, (latt, nproj, same) in enumerate(cases):
         latt = tuple(latt)
         projs = pp if nproj == 2 else g4  # (1 +- g4)/2: two gamma-basis terms; g4: one
         props = [eo.make_propagator(latt, 500 + 3 * k + s, 0.25) for s in range(3)]
+        if same:
+            props[1] = props[0]
         site = np.array([[oracle.baryon_general_two_point(*props, t, 5, 5, projs[w]) for w in range(nproj)]
                          for t in range(6)])
         ref = eo.timeslice_sum(site, latt)
         sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real)
         dev = [torch.from_numpy(p).cuda().to(torch.complex64) for p in props]
+        if same:
+            dev[1] = dev[0]
         got = api.baryon_all_types(*dev, 5, 5, projs, latt=latt).cpu().numpy()
         if lib.contract_last_error():
             raise RuntimeError(lib.contract_last_error_message().decode())

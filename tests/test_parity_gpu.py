@@ -201,10 +201,20 @@ def test_fused_same_field_for_i_and_j(api, props, c_oracle):
     # one projector; phased gammas; a dense projector (the two-pass general form)
     rng = np.random.default_rng(17)
     dense = (rng.standard_normal(16) + 1j * rng.standard_normal(16)).reshape(1, 16)
-    for gij, gkl, projs in ((5, 5, pp[:1]), (13, 10, pp), (5, 5, dense)):
+    # (15: g5 is diagonal, a Gamma_ij permutation with fixed points -> the merged one-pass form)
+    for gij, gkl, projs in ((5, 5, pp[:1]), (13, 10, pp), (5, 5, dense), (15, 5, pp), (0, 13, pp)):
         s1 = api.baryon_all_types(a, a, c, gij, gkl, projs, latt=LATT).cpu().numpy()
         t1 = api.baryon_all_types(a, a.clone(), c, gij, gkl, projs, latt=LATT).cpu().numpy()
-        assert np.abs(s1 - t1).max() <= 1e-6 * np.abs(t1).max(), (gij, gkl, projs.shape)
+        # some types vanish identically for one field (e.g. with Gamma_ij = g5): their
+        # FP32 values are rounding noise, measured on the scale of the case's
+        # largest per-timeslice spread
+        sites = np.array([[c_oracle.baryon_general_two_point(pi, pi, pn, t, gij, gkl, projs[w])
+                           for w in range(projs.shape[0])] for t in range(6)])
+        ref = eo.timeslice_sum(sites, LATT)
+        scale = np.sqrt(eo.timeslice_sum(np.abs(sites) ** 2, LATT).real).max(axis=(0, 1))
+        for got in (s1, t1):
+            err = np.abs(got - ref) / np.maximum(np.abs(ref), scale)
+            assert err.max() < TOL_C64_TIMESLICE, (gij, gkl, err.max())
     for t in range(6):
         for w in range(2):
             site = c_oracle.baryon_general_two_point(pi, pi, pn, t, 5, 5, pp[w])
@@ -433,9 +443,10 @@ def test_meson_momentum_many_z_groups(api):
 
 def test_fused_variants_forced(tmp_path):
     """Every compiled tile-shape variant of the complex64 fused all-types pass
-    (shared-wedge, merged and two-loop forms; two and one projector), forced
-    through a tune cache, against the FP64 oracle.  Each case uses its own
-    lattice shape, so that each tune key fixes one variant."""
+    (shared-wedge, merged and two-loop forms; two and one projector; two
+    fields and one field for P_i and P_j), forced through a tune cache, against
+    the FP64 oracle.  Each case uses its own lattice shape, so that each tune
+    key fixes one variant."""
     import ctypes
     import json
     import os
@@ -446,17 +457,18 @@ def test_fused_variants_forced(tmp_path):
     lib = _lib.lib()
     cache = tmp_path / "tune.txt"
     lines, cases, names = [], [], []
-    for nproj in (2, 1):
+    for nproj, same in ((2, False), (1, False), (2, True), (1, True)):
+        aux = nproj + (4 if same else 0)
         buf = ctypes.create_string_buffer(4096)
-        n = lib.contract_variant_names(3, 1, nproj, buf, len(buf))  # op 3: the fused all-types pass
+        n = lib.contract_variant_names(3, 1, aux, buf, len(buf))  # op 3: the fused all-types pass
         vnames = buf.value.decode().split()
-        assert n == len(vnames) >= 8, (n, vnames)
+        assert n == len(vnames) >= 7, (n, vnames)
         for v, name in enumerate(vnames):
-            latt = (4, 2, 2, 2 + v) if nproj == 2 else (2, 4, 2, 2 + v)
+            latt = (4, 2, 2 + 2 * same, 2 + v) if nproj == 2 else (2, 4, 2 + 2 * same, 2 + v)
             vol = int(np.prod(latt))
-            key = f"kind=3,prec=1,aux={nproj},volume={vol},lt={latt[3]},half={vol // latt[3] // 2}"
+            key = f"kind=3,prec=1,aux={aux},volume={vol},lt={latt[3]},half={vol // latt[3] // 2}"
             lines.append(f"{key}\t{v} {name} 1.0\n")
-            cases.append([list(latt), nproj])
+            cases.append([list(latt), nproj, same])
             names.append(name)
     cache.write_text("".join(lines))
     env = dict(os.environ, CONTRACT_TUNE_CACHE=str(cache), CONTRACT_AUTOTUNE="0")
@@ -571,8 +583,11 @@ def test_batched_work_queue_and_cuda_graph(api, c64):
     lib.contract_baryon_all_types_batch(arr, len(outs), 5, 5, 2, pp.ctypes.data, prec)
     torch.cuda.synchronize()
     assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+    # complex64: the per-item calls may run another tile shape (autotuned), so
+    # the FP32 partial sums group differently
+    tol = 1e-6 if c64 else 1e-12
     for out, ref in zip(outs, refs):
-        assert rel_err(out.cpu().numpy(), ref) < 1e-12
+        assert rel_err(out.cpu().numpy(), ref) < tol
     # capture the same launch in a CUDA graph and replay it
     for out in outs:
         out.fill_(float("nan"))
@@ -593,7 +608,7 @@ def test_batched_work_queue_and_cuda_graph(api, c64):
     torch.cuda.synchronize()
     assert lib.contract_last_error() == 0, lib.contract_last_error_message()
     for out, ref in zip(outs, refs):
-        assert rel_err(out.cpu().numpy(), ref) < 1e-12
+        assert rel_err(out.cpu().numpy(), ref) < tol
     api.check_device()
 
 
