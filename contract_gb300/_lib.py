@@ -53,6 +53,9 @@ SIGNATURES = {
     "contract_gamma_table": (None, [c_int_p, c_int_p]),
     "contract_convert_precision": (None, [c_void_p, c_void_p, c_size_t, c_int]),
     "contract_convert_layout": (None, [c_void_p, c_void_p, c_int_p, c_int, c_int]),
+    "contract_convert_from_quda": (None, [c_void_p, ctypes.POINTER(c_void_p), c_int_p, c_size_t, c_int]),
+    "contract_convert_to_quda": (None, [ctypes.POINTER(c_void_p), c_void_p, c_int_p, c_size_t, c_int]),
+    "contract_rotate_spin_basis": (None, [c_void_p, c_size_t, c_void_p, c_int]),
     "contract_meson": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, c_int, c_int_p]),
     "contract_meson_all": (None, [ctypes.POINTER(c_void_p), c_void_p, c_void_p, c_size_t, c_int, c_int, c_int,
                                   c_int_p]),
@@ -67,6 +70,9 @@ SIGNATURES = {
     "contract_baryon_all_types_batch": (None, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "contract_meson_all_gamma_momentum": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int_p, c_int_p, c_int,
                                                  c_int]),
+    "contract_meson_all_gamma_momentum_batch": (None, [c_void_p, c_int, c_int_p, c_int, c_int]),
+    "contract_batch_mixed": (None, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int_p, c_int,
+                                    c_int]),
     "contract_diquark": (None, [c_void_p, c_void_p, c_void_p, c_size_t, c_int, c_int, c_int]),
     "contract_sequential_sink": (None, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_size_t, c_int_p, c_int, c_int,
                                         c_int, c_int, c_int]),

@@ -121,6 +121,65 @@ def baryon_all_types(propag_i, propag_j, propag_n, gamma_ij, gamma_kl, projector
     return out
 
 
+def _quda_fields(fields, latt, stride, dtype):
+    torch = _torch()
+    if len(fields) != 12:
+        raise ValueError("a propagator is 12 QUDA colour-spinor fields (source spin k, colour d: field 3k + d)")
+    half = int(np.prod([int(x) for x in latt])) // 2
+    stride = int(stride) if stride else half
+    need = 2 * 12 * stride  # complex entries per field: [2][chunks][stride][16 B]
+    for f in fields:
+        if not isinstance(f, torch.Tensor) or not f.is_cuda or not f.is_contiguous() or f.dtype != dtype:
+            raise TypeError(f"QUDA fields must be contiguous CUDA tensors of {dtype}")
+        if f.numel() < need:
+            raise ValueError(f"QUDA field holds {f.numel()} complex entries, needs {need}")
+    arr = (ctypes.c_void_p * 12)(*[f.data_ptr() for f in fields])
+    return arr, stride
+
+
+def from_quda(fields, latt, stride=0, out=None):
+    """Propagator [V, 4, 4, 3, 3] in PyQUDA even/odd order from QUDA's 12
+    native-order colour-spinor fields (complex128: FLOAT2 order; complex64:
+    FLOAT4 order), each [2][chunks][stride][16 bytes]."""
+    torch = _torch()
+    dtype = fields[0].dtype
+    arr, stride = _quda_fields(fields, latt, stride, dtype)
+    v = int(np.prod([int(x) for x in latt]))
+    if out is None:
+        out = torch.empty((v, 4, 4, 3, 3), dtype=dtype, device=fields[0].device)
+    lib = _lib_record()
+    lib.contract_convert_from_quda(_ptr(out), arr, _latt(latt), stride,
+                                   CONTRACT_C128 if dtype == torch.complex128 else CONTRACT_C64)
+    _check(lib)
+    return out
+
+
+def to_quda(propag, latt, stride=0):
+    """The 12 QUDA native-order colour-spinor fields of a PyQUDA even/odd
+    propagator; each field is a flat tensor of 2 * 12 * stride complex entries
+    whose pad sites (beyond V/2 in each parity) are zero."""
+    torch = _torch()
+    v = _volume(propag)
+    half = v // 2
+    stride = int(stride) if stride else half
+    fields = [torch.zeros(2 * 12 * stride, dtype=propag.dtype, device=propag.device) for _ in range(12)]
+    arr, stride = _quda_fields(fields, latt, stride, propag.dtype)
+    lib = _lib_record()
+    lib.contract_convert_to_quda(arr, _ptr(propag), _latt(latt), stride, _prec(propag))
+    _check(lib)
+    return fields
+
+
+def rotate_spin_basis(propag, rotation):
+    """In place P -> U P U^dagger on both spin indices (U: 4 x 4 complex)."""
+    v = _volume(propag)
+    u = np.ascontiguousarray(np.asarray(rotation, dtype=np.complex128).reshape(4, 4))
+    lib = _lib_record()
+    lib.contract_rotate_spin_basis(_ptr(propag), v, u.ctypes.data, _prec(propag))
+    _check(lib)
+    return propag
+
+
 def set_stream(stream):
     """Queue library work on a torch.cuda.Stream (or raw cudaStream_t int); None = legacy default."""
     lib = _lib.lib()

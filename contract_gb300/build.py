@@ -34,6 +34,7 @@ SOURCES = [
     "kernels_momentum_fused.cu",
     "kernels_batch.cu",
     "noalloc.cu",
+    "kernels_quda.cu",
 ]
 
 

@@ -15,6 +15,8 @@
 #include <cstring>
 #include <cmath>
 #include <fstream>
+#include <functional>
+#include <memory>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -56,6 +58,11 @@ struct DevState {
   size_t pipe_bytes = 0;
   cudaStream_t copy = nullptr;  // host-to-device copies of the host-input pipeline
   cudaEvent_t copied[kPipeSlots] = {}, freed[kPipeSlots] = {}, start = nullptr;
+  // Tensor-core momentum projection: the phase tiles of the last (lattice,
+  // momentum list), kept so that repeated calls do not rebuild them.
+  void *tc_tiles = nullptr;
+  size_t tc_tiles_bytes = 0;
+  std::string tc_key;
 };
 DevState g_dev[64];
 std::mutex g_dev_mu;  // guards the first-use set-up of g_dev entries
@@ -186,6 +193,8 @@ struct TuneEntry {
 struct Tuner {
   std::mutex mu;
   std::map<std::string, TuneEntry> choice;
+  // batched launches: per lattice class, the time of every tile shape
+  std::map<std::string, std::vector<float>> class_ms;
   int enabled = -1;
   bool loaded = false;
   std::string path;
@@ -285,6 +294,92 @@ template <class Launch> cudaError_t tuned_launch(cgb::Kind kind, cgb::Job job, i
   }
   job.variant = v;
   return launch(job);
+}
+
+// Tile shape of a batched launch, tuned per lattice extent: each class of
+// items (one lattice shape) is timed alone under every shape (one item of
+// the class, a warm-up run and two timed runs), which gives that class's
+// best shape in the report; one launch serves every item, so the batch takes
+// the shape with the least sum over its items of their class's time.
+// classes: (class key, item count); run_one(c, v) runs one item of class c
+// under shape v.  Returns the shape, or -1 (the launcher's default) when
+// tuning is off and nothing is cached.
+int tune_batch(const std::string &tag, int nvariants, const char *const *names,
+               const std::vector<std::pair<std::string, int>> &classes,
+               const std::function<cudaError_t(int, int)> &run_one, cudaStream_t stream)
+{
+  std::string comp = tag + ",batch=";
+  for (const auto &c : classes) comp += c.first + "x" + std::to_string(c.second) + ";";
+  std::vector<std::vector<float>> times(classes.size());
+  bool have_all = true;
+  {
+    std::lock_guard<std::mutex> lk(g_tune.mu);
+    tune_load_locked();
+    for (size_t c = 0; c < classes.size(); ++c) {
+      auto it = g_tune.class_ms.find(tag + ",latt=" + classes[c].first);
+      if (it != g_tune.class_ms.end() && (int)it->second.size() == nvariants) times[c] = it->second;
+      else have_all = false;
+    }
+    if (!have_all) {
+      auto it = g_tune.choice.find(comp);
+      if (it != g_tune.choice.end() && it->second.variant < nvariants && it->second.name == names[it->second.variant])
+        return it->second.variant;
+    }
+  }
+  if (!have_all) {
+    if (!autotune_enabled() || stream_capturing(stream)) return -1;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return -1;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      return -1;
+    }
+    for (size_t c = 0; c < classes.size(); ++c) {
+      if (!times[c].empty()) continue;
+      std::vector<float> ms(nvariants, INFINITY);
+      for (int v = 0; v < nvariants; ++v) {
+        if (run_one((int)c, v) != cudaSuccess) continue;
+        cudaEventRecord(e0, stream);
+        cudaError_t e = run_one((int)c, v);
+        if (e == cudaSuccess) e = run_one((int)c, v);
+        cudaEventRecord(e1, stream);
+        if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) continue;
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        ms[v] = t / 2;
+      }
+      times[c] = ms;
+      const int best = (int)(std::min_element(ms.begin(), ms.end()) - ms.begin());
+      const std::string key = tag + ",latt=" + classes[c].first;
+      std::lock_guard<std::mutex> lk(g_tune.mu);
+      g_tune.class_ms[key] = ms;
+      g_tune.choice[key] = {best, ms[best], names[best]};
+      if (!g_tune.path.empty()) {
+        std::ofstream f(g_tune.path, std::ios::app);
+        f << key << '\t' << best << ' ' << names[best] << ' ' << ms[best] << '\n';
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  int v = 0;
+  float best = INFINITY;
+  for (int cand = 0; cand < nvariants; ++cand) {
+    float sum = 0;
+    for (size_t c = 0; c < classes.size(); ++c) sum += classes[c].second * times[c][cand];
+    if (sum < best) {
+      best = sum;
+      v = cand;
+    }
+  }
+  if (!std::isfinite(best)) return -1;
+  std::lock_guard<std::mutex> lk(g_tune.mu);
+  g_tune.choice[comp] = {v, best, names[v]};
+  if (!g_tune.path.empty()) {
+    std::ofstream f(g_tune.path, std::ios::app);
+    f << comp << '\t' << v << ' ' << names[v] << ' ' << best << '\n';
+  }
+  return v;
 }
 
 bool gamma_ok(int g, const char *name)
@@ -774,6 +869,296 @@ bool pipeline_ready(DevState *s, size_t bytes)
   return true;
 }
 
+// ------------------------------------------------------ batched launches --
+struct BaryonBatch {
+  std::vector<cgb::BatchSpec> specs;
+  OpParams<double> p {};
+};
+
+// Validates baryon batch items and builds the launch's specs and spin tables.
+bool baryon_batch_setup(BaryonBatch &bb, const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,
+                        int nproj, const void *projectors, int precision)
+{
+  if (nitems < 0 || nitems > 128) return invalid("nitems must be 0..128 (got %d)", nitems);
+  if (!items || !projectors) return invalid("items and projectors are required");
+  if (nproj < 1 || nproj > 2) return invalid("nproj must be 1 or 2 (got %d)", nproj);
+  if (!gamma_ok(gamma_ij, "gamma_ij") || !gamma_ok(gamma_kl, "gamma_kl") || !prec_ok(precision)) return false;
+  bb.specs.assign(nitems, cgb::BatchSpec {});
+  for (int i = 0; i < nitems; ++i) {
+    const ContractBaryonBatchItem &it = items[i];
+    const int *l = it.lattice;
+    if (l[0] <= 0 || l[1] <= 0 || l[2] <= 0 || l[3] <= 0 || (l[0] & 1))
+      return invalid("batch item %d: invalid lattice {%d, %d, %d, %d}", i, l[0], l[1], l[2], l[3]);
+    const size_t v = (size_t)l[0] * l[1] * l[2] * l[3];
+    if (!ptr_ok(it.correl, v, "correl") || !ptr_ok(it.propag_i, v, "propag_i") ||
+        !ptr_ok(it.propag_j, v, "propag_j") || !ptr_ok(it.propag_n, v, "propag_n"))
+      return false;
+    cgb::BatchSpec &sp = bb.specs[i];
+    sp.in[0] = it.propag_i;
+    sp.in[1] = it.propag_j;
+    sp.in[2] = it.propag_n;
+    sp.out = static_cast<double2 *>(it.correl);
+    for (int k = 0; k < 4; ++k) sp.latt[k] = l[k];
+  }
+  OpParams<double> &p = bb.p;
+  p = {};
+  set_row(p.b.perm1, kG.perm[gamma_ij]);
+  set_row(p.b.perm2, kG.perm[gamma_kl]);
+  set_row(p.b.ph1[0], kG.ph[gamma_ij]);
+  set_row(p.b.ph1[1], kG.ph_t[gamma_ij]);
+  set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);
+  set_row(p.b.ph2[1], kG.ph[gamma_kl]);
+  const double *pr = static_cast<const double *>(projectors);
+  const double *pw[2] = {pr, pr + 32};
+  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
+  fill_clifford(p.b.cl, pw, nproj, 0);
+  if (p.b.cl.ng > nproj)
+    return invalid("batched contractions need projectors spanned by at most nproj gamma matrices (got %d terms)",
+                   p.b.cl.ng);
+  return true;
+}
+
+// Validates meson momentum batch items and fills the launch parameters (all
+// but the plane buffers).  Every item's momentum plan must have the structure
+// of the first item's (true for any list of components n with 2|n| < L in
+// every direction); phase tables are kept once per distinct extent.
+bool meson_batch_setup(cgb::MomBatchParams &mp, size_t &plane_floats, const ContractMesonMomentumBatchItem *items,
+                       int nitems, const int *moms, int nmom)
+{
+  if (nitems < 0 || nitems > cgb::kMomBatchMaxItems)
+    return invalid("nmeson must be 0..%d (got %d)", cgb::kMomBatchMaxItems, nitems);
+  mp = {};
+  plane_floats = 0;
+  if (nitems == 0) return true;
+  if (!items || !moms) return invalid("meson items and moms are required");
+  std::vector<int> ext;  // distinct extents
+  auto ext_index = [&](int L) {
+    for (size_t e = 0; e < ext.size(); ++e)
+      if (ext[e] == L) return (int)e;
+    ext.push_back(L);
+    return (int)ext.size() - 1;
+  };
+  cgb::MomPlan first;
+  int units = 0, fin = 0;
+  for (int i = 0; i < nitems; ++i) {
+    const ContractMesonMomentumBatchItem &it = items[i];
+    const int *l = it.lattice;
+    if (l[0] <= 0 || l[1] <= 0 || l[2] <= 0 || l[3] <= 0 || (l[0] & 1))
+      return invalid("meson item %d: invalid lattice {%d, %d, %d, %d}", i, l[0], l[1], l[2], l[3]);
+    const size_t v = (size_t)l[0] * l[1] * l[2] * l[3];
+    if (!ptr_ok(it.correl, v, "correl") || !ptr_ok(it.propag_i, v, "propag_i") || !ptr_ok(it.propag_j, v, "propag_j"))
+      return false;
+    cgb::MomPlan plan;
+    if (!make_mom_plan(plan, l, moms, nmom)) return false;
+    if (i == 0) {
+      first = plan;
+      if (!cgb::momentum_fused_supported(plan))
+        return invalid("batched momentum projection supports up to 3 X groups and %d (nx, ny) pairs", cgb::kMomQChunk);
+      if (plan.q_g0[plan.nq] > cgb::kMomBatchMaxG)
+        return invalid("batched momentum projection supports up to %d z groups", cgb::kMomBatchMaxG);
+    } else {
+      bool same = plan.npx == first.npx && plan.nq == first.nq && plan.ngx == first.ngx;
+      for (int k = 0; same && k < plan.ngx; ++k)
+        same = plan.gx_k[k] == first.gx_k[k] && plan.gx_plus[k] == first.gx_plus[k] &&
+               plan.gx_minus[k] == first.gx_minus[k];
+      for (int q = 0; same && q <= plan.nq; ++q) same = plan.q_g0[q] == first.q_g0[q];
+      for (int q = 0; same && q < plan.nq; ++q) same = plan.q_ix[q] == first.q_ix[q] && plan.q_ny[q] == first.q_ny[q];
+      for (int g = 0; same && g < plan.q_g0[plan.nq]; ++g)
+        same = plan.gz_k[g] == first.gz_k[g] && plan.gz_plus[g] == first.gz_plus[g] &&
+               plan.gz_minus[g] == first.gz_minus[g];
+      if (!same)
+        return invalid("meson item %d: the momentum list has another structure on lattice {%d, %d, %d, %d} "
+                       "than on the first item's", i, l[0], l[1], l[2], l[3]);
+    }
+    cgb::MomBatchItem &b = mp.items[i];
+    b.in[0] = static_cast<const char *>(it.propag_i);
+    b.in[1] = static_cast<const char *>(it.propag_j);
+    b.out = static_cast<double2 *>(it.correl);
+    for (int k = 0; k < 4; ++k) b.latt[k] = l[k];
+    b.unit_begin = units;
+    b.tpp = (l[0] * l[1] + 15) / 16;
+    b.fin_begin = fin;
+    const int ex = ext_index(l[0]), ey = ext_index(l[1]), ez = ext_index(l[2]);
+    if ((int)ext.size() > cgb::kMomBatchMaxExt)
+      return invalid("batched momentum projection supports up to %d distinct spatial extents", cgb::kMomBatchMaxExt);
+    b.tx = (uint8_t)ex;
+    b.ty = (uint8_t)ey;
+    b.tz = (uint8_t)ez;
+    // the phase tables of the per-call plan, FP32 as the kernels use them
+    for (int k = 0; k < l[0]; ++k) mp.tab[ex][k] = make_float2((float)plan.cosx[k], (float)plan.sinx[k]);
+    for (int k = 0; k < l[1]; ++k) mp.tab[ey][k] = make_float2((float)plan.cosy[k], (float)plan.siny[k]);
+    for (int k = 0; k < l[2]; ++k) mp.tab[ez][k] = make_float2((float)plan.cosz[k], (float)plan.sinz[k]);
+    units += l[2] * l[3];
+    fin += first.nq * l[3];
+    plane_floats += (size_t)l[2] * l[3] * first.nq * 256 * 2;
+  }
+  mp.n_items = nitems;
+  mp.total_units = units;
+  mp.total_fin = fin;
+  mp.ngx = first.ngx;
+  mp.nq = first.nq;
+  mp.np = first.np;
+  for (int k = 0; k < first.ngx; ++k) {
+    mp.gx_k[k] = first.gx_k[k];
+    mp.gx_plus[k] = first.gx_plus[k];
+    mp.gx_minus[k] = first.gx_minus[k];
+  }
+  for (int q = 0; q < first.nq; ++q) {
+    mp.q_ix[q] = first.q_ix[q];
+    mp.q_ny[q] = first.q_ny[q];
+  }
+  for (int q = 0; q <= first.nq; ++q) mp.q_g0[q] = first.q_g0[q];
+  for (int g = 0; g < first.q_g0[first.nq]; ++g) {
+    mp.gz_k[g] = first.gz_k[g];
+    mp.gz_plus[g] = first.gz_plus[g];
+    mp.gz_minus[g] = first.gz_minus[g];
+  }
+  return true;
+}
+
+std::string latt_key(const int *l)
+{
+  return std::to_string(l[0]) + "," + std::to_string(l[1]) + "," + std::to_string(l[2]) + "," + std::to_string(l[3]);
+}
+
+// A workspace view `off` bytes into another (the momentum planes sit below
+// the baryon partials of a mixed batch).
+struct OffsetWorkspace : cgb::Workspace {
+  cgb::Workspace *base;
+  size_t off;
+  OffsetWorkspace(cgb::Workspace *b, size_t o) : base(b), off(o) { }
+  void *get(size_t bytes) override
+  {
+    char *p = static_cast<char *>(base->get(off + bytes));
+    return p ? p + off : nullptr;
+  }
+};
+
+// Baryon items and meson momentum items (complex64), each kind in one
+// persistent launch with its tile shape tuned per extent, then one combined
+// finalisation launch.
+void run_mixed_batch(const ContractBaryonBatchItem *bitems, int nb, int gamma_ij, int gamma_kl, int nproj,
+                     const void *projectors, const ContractMesonMomentumBatchItem *mitems, int nm, const int *moms,
+                     int nmom, int precision, const char *what)
+{
+  if (precision != CONTRACT_C64) {
+    invalid("%s needs CONTRACT_C64 propagators (got precision %d)", what, precision);
+    return;
+  }
+  if (nb < 0 || nb > 128 || nm < 0 || nm > cgb::kMomBatchMaxItems) {
+    invalid("%s: item counts must be 0..128 (got %d baryon, %d meson)", what, nb, nm);
+    return;
+  }
+  BaryonBatch bb;
+  if (nb > 0 && !baryon_batch_setup(bb, bitems, nb, gamma_ij, gamma_kl, nproj, projectors, precision)) return;
+  auto mp = std::make_unique<cgb::MomBatchParams>();
+  size_t plane_floats = 0;
+  if (!meson_batch_setup(*mp, plane_floats, mitems, nm, moms, nmom)) return;
+  if (nb == 0 && nm == 0) return;
+  cgb::Job job;
+  DevState *s = nullptr;
+  if (!make_job(job, precision, 0, nullptr, &s)) return;
+  DeviceWorkspace ws(s);
+  const size_t plane_bytes = (plane_floats * sizeof(float) + 255) / 256 * 256;
+  OffsetWorkspace bws(&ws, plane_bytes);
+  mp->status = job.status;
+
+  // per-extent tile shapes
+  int bvar = -1, mvar = -1;
+  const bool msame = [&] {
+    bool same = nm > 0;
+    for (int i = 0; i < nm; ++i) same = same && mitems[i].propag_i == mitems[i].propag_j;
+    return same;
+  }();
+  if (nb > 0) {
+    const bool same = cgb::batch_same_field(bb.p, bb.specs.data(), nb);
+    const char *const *names = nullptr;
+    const int nv = cgb::batch_variants(same, &names);
+    std::vector<std::pair<std::string, int>> classes;
+    std::vector<int> rep;  // first item of each class
+    for (int i = 0; i < nb; ++i) {
+      const std::string k = latt_key(bb.specs[i].latt);
+      auto it = std::find_if(classes.begin(), classes.end(), [&](const auto &c) { return c.first == k; });
+      if (it == classes.end()) {
+        classes.push_back({k, 1});
+        rep.push_back(i);
+      } else {
+        ++it->second;
+      }
+    }
+    const std::string tag = std::string("batch=baryon,nproj=") + std::to_string(nproj) + ",same=" + (same ? "1" : "0");
+    cgb::Job tj = job;
+    tj.ws = &bws;
+    bvar = tune_batch(tag, nv, names, classes, [&](int c, int v) {
+      tj.variant = v;
+      return cgb::launch_baryon_fused_batch(tj, nproj, bb.p, &bb.specs[rep[c]], 1);
+    }, job.stream);
+  }
+  if (nm > 0) {
+    static const char *const kMomBatchNames[] = {"fused.site8.xy8", "fused.site16.xy8"};
+    std::vector<std::pair<std::string, int>> classes;
+    std::vector<int> rep;
+    for (int i = 0; i < nm; ++i) {
+      const std::string k = latt_key(mitems[i].lattice);
+      auto it = std::find_if(classes.begin(), classes.end(), [&](const auto &c) { return c.first == k; });
+      if (it == classes.end()) {
+        classes.push_back({k, 1});
+        rep.push_back(i);
+      } else {
+        ++it->second;
+      }
+    }
+    const std::string tag = std::string("batch=meson_momentum,nmom=") + std::to_string(nmom) +
+                            ",same=" + (msame ? "1" : "0");
+    auto one = std::make_unique<cgb::MomBatchParams>();
+    mvar = tune_batch(tag, 2, kMomBatchNames, classes, [&](int c, int v) {
+      // one item of class c alone: its own plane buffer at the workspace start
+      *one = *mp;
+      one->n_items = 1;
+      one->items[0] = mp->items[rep[c]];
+      one->items[0].unit_begin = 0;
+      one->items[0].fin_begin = 0;
+      const int *l = one->items[0].latt;
+      one->total_units = l[2] * l[3];
+      one->total_fin = mp->nq * l[3];
+      float2 *pl = static_cast<float2 *>(ws.get((size_t)l[2] * l[3] * mp->nq * 256 * sizeof(float2)));
+      if (!pl) return cudaErrorMemoryAllocation;
+      one->items[0].planes = pl;
+      cudaError_t e = cgb::launch_momentum_batch(job, *one, msame, v == 1 ? 16 : 8);
+      if (e != cudaSuccess) return e;
+      cgb::BaryonFinParams none {};
+      return cgb::launch_batch_finalize(job, *one, none);
+    }, job.stream);
+  }
+
+  // the launches: baryon items, meson items, one finalisation
+  auto bf = std::make_unique<cgb::BaryonFinParams>();
+  *bf = {};
+  if (nb > 0) {
+    cgb::Job bj = job;
+    bj.ws = &bws;
+    bj.variant = bvar;
+    if (!cuda_ok(cgb::launch_baryon_fused_batch(bj, nproj, bb.p, bb.specs.data(), nb, bf.get()), what)) return;
+  }
+  if (nm > 0) {
+    // after the baryon launch's workspace request, so this one does not move the buffer
+    char *planes = static_cast<char *>(ws.get(plane_bytes));
+    if (!planes) {
+      fail(CONTRACT_ERROR_OUT_OF_MEMORY, (int)cudaErrorMemoryAllocation, "%s: workspace of %zu bytes", what,
+           plane_bytes);
+      return;
+    }
+    size_t off = 0;
+    for (int i = 0; i < nm; ++i) {
+      mp->items[i].planes = reinterpret_cast<float2 *>(planes + off);
+      const int *l = mp->items[i].latt;
+      off += (size_t)l[2] * l[3] * mp->nq * 256 * sizeof(float2);
+    }
+    if (!cuda_ok(cgb::launch_momentum_batch(job, *mp, msame, mvar == 1 ? 16 : 8), what)) return;
+  }
+  cuda_ok(cgb::launch_batch_finalize(job, *mp, *bf), what);
+}
+
 } // namespace
 
 // Only the C ABI is exported (the library is built with -fvisibility=hidden).
@@ -976,6 +1361,90 @@ void contract_convert_layout(void *dst, const void *src, const int *lattice, int
   if (!make_job(job, precision, volume, lattice)) return;
   cuda_ok(cgb::launch_layout(job, dst, src, lattice, to_eo != 0, precision == CONTRACT_C64 ? 1152 : 2304),
           "contract_convert_layout");
+}
+
+// Shared checks of the QUDA-order conversions: the lattice, the stride, the
+// twelve field pointers (16-byte aligned, disjoint from each other and from
+// the propagator).  Returns the stride in 16-byte chunks, or -1.
+static long long quda_fields_ok(void *const *fields, const void *propag, const int *lattice, size_t stride,
+                                int precision, size_t &volume)
+{
+  if (!lattice) {
+    invalid("the QUDA-order conversions need the lattice");
+    return -1;
+  }
+  if (!prec_ok(precision)) return -1;
+  volume = (size_t)std::max(0, lattice[0]) * std::max(0, lattice[1]) * std::max(0, lattice[2]) *
+           std::max(0, lattice[3]);
+  const size_t half = volume / 2;
+  if (stride == 0) stride = half;
+  if (stride < half) {
+    invalid("QUDA field stride %zu is shorter than the checkerboard length %zu", stride, half);
+    return -1;
+  }
+  if (!fields) {
+    invalid("fields is NULL (a host array of 12 device pointers)");
+    return -1;
+  }
+  if (!ptr_ok(propag, volume, "propagator")) return -1;
+  const size_t esz = precision == CONTRACT_C64 ? 8 : 16;
+  const size_t fbytes = 2 * 12 * esz * stride;  // [2 parities][12 entries * esz / 16 chunks][stride][16 B]
+  const size_t pbytes = volume * 144 * esz;
+  for (int k = 0; k < 12; ++k) {
+    if (!ptr_ok(fields[k], volume, "QUDA field")) return -1;
+    if (!volume) continue;
+    const char *a = static_cast<const char *>(fields[k]), *p = static_cast<const char *>(propag);
+    if (a < p + pbytes && p < a + fbytes) {
+      invalid("QUDA field %d overlaps the propagator", k);
+      return -1;
+    }
+    for (int j = 0; j < k; ++j) {
+      const char *b = static_cast<const char *>(fields[j]);
+      if (a < b + fbytes && b < a + fbytes) {
+        invalid("QUDA fields %d and %d overlap", j, k);
+        return -1;
+      }
+    }
+  }
+  return (long long)stride;
+}
+
+void contract_convert_from_quda(void *propag, void *const *fields, const int *lattice, size_t stride, int precision)
+{
+  size_t volume = 0;
+  const long long st = quda_fields_ok(fields, propag, lattice, stride, precision, volume);
+  if (st < 0) return;
+  cgb::Job job;
+  if (!make_job(job, precision, volume, lattice)) return;
+  cuda_ok(cgb::launch_quda_layout(job, propag, fields, st, true, precision == CONTRACT_C64 ? 8 : 16),
+          "contract_convert_from_quda");
+}
+
+void contract_convert_to_quda(void *const *fields, const void *propag, const int *lattice, size_t stride,
+                              int precision)
+{
+  size_t volume = 0;
+  const long long st = quda_fields_ok(fields, propag, lattice, stride, precision, volume);
+  if (st < 0) return;
+  cgb::Job job;
+  if (!make_job(job, precision, volume, lattice)) return;
+  cuda_ok(cgb::launch_quda_layout(job, const_cast<void *>(propag), fields, st, false,
+                                  precision == CONTRACT_C64 ? 8 : 16),
+          "contract_convert_to_quda");
+}
+
+void contract_rotate_spin_basis(void *propag, size_t volume, const void *rotation, int precision)
+{
+  if (!prec_ok(precision)) return;
+  if (!rotation) {
+    invalid("rotation is NULL (a host array of 16 complex128)");
+    return;
+  }
+  if (!ptr_ok(propag, volume, "propagator")) return;
+  cgb::Job job;
+  if (!make_job(job, precision, volume, nullptr)) return;
+  cuda_ok(cgb::launch_spin_rotation(job, propag, static_cast<const double *>(rotation)),
+          "contract_rotate_spin_basis");
 }
 
 void contract_meson(void *correl, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
@@ -1206,67 +1675,64 @@ void contract_meson_all_gamma_momentum(void *correl, const void *propag_i, const
   p.in[1] = propag_j;
   const bool fused = job.prec == cgb::Prec::C64 && cgb::momentum_fused_supported(plan);
   const int aux = tensor_cores ? 2 : (fused ? 1 + (propag_i == propag_j ? 4 : 0) : 0);
-  cuda_ok(tuned_launch(cgb::Kind::Momentum, job, aux,
-                       [&](const cgb::Job &j) { return cgb::launch_meson_momentum(j, p, plan, correl, tensor_cores); }),
-          "contract_meson_all_gamma_momentum");
+  std::string tc_key;
+  if (tensor_cores && volume) {
+    // phase tiles: rebuilt only when the lattice or the momentum list changes
+    tc_key = std::to_string(lattice[0]) + "," + std::to_string(lattice[1]) + "," + std::to_string(lattice[2]) + ":";
+    for (int k = 0; k < 3 * nmom; ++k) tc_key += std::to_string(moms[k]) + ",";
+    const size_t need = cgb::tc_phase_bytes(cgb::make_tc_geom(plan));
+    if (s->tc_tiles_bytes < need) {
+      if (s->tc_tiles) {
+        if (!cuda_ok(cudaDeviceSynchronize(), "contract_meson_all_gamma_momentum")) return;
+        cudaFree(s->tc_tiles);
+        s->tc_tiles = nullptr;
+        s->tc_tiles_bytes = 0;
+      }
+      if (cudaMalloc(&s->tc_tiles, need) != cudaSuccess) {
+        s->tc_tiles = nullptr;
+        fail(CONTRACT_ERROR_OUT_OF_MEMORY, (int)cudaErrorMemoryAllocation, "phase tiles of %zu bytes", need);
+        return;
+      }
+      s->tc_tiles_bytes = need;
+      s->tc_key.clear();
+    }
+    job.tc_tiles = s->tc_tiles;
+    job.tc_tiles_ready = s->tc_key == tc_key;
+  }
+  const bool ok = cuda_ok(
+    tuned_launch(cgb::Kind::Momentum, job, aux,
+                 [&](const cgb::Job &j) { return cgb::launch_meson_momentum(j, p, plan, correl, tensor_cores); }),
+    "contract_meson_all_gamma_momentum");
+  if (tensor_cores && volume) s->tc_key = ok ? tc_key : std::string();
 }
 
 void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,
                                      int nproj, const void *projectors, int precision)
 {
-  if (nitems < 0 || nitems > 128) {
-    invalid("nitems must be 0..128 (got %d)", nitems);
-    return;
-  }
   if (nitems == 0) return;
-  if (!items || !projectors) {
-    invalid("items and projectors are required");
-    return;
-  }
-  if (nproj < 1 || nproj > 2) {
-    invalid("nproj must be 1 or 2 (got %d)", nproj);
-    return;
-  }
-  if (!gamma_ok(gamma_ij, "gamma_ij") || !gamma_ok(gamma_kl, "gamma_kl") || !prec_ok(precision)) return;
-  std::vector<cgb::BatchSpec> specs(nitems);
-  for (int i = 0; i < nitems; ++i) {
-    const ContractBaryonBatchItem &it = items[i];
-    const int *l = it.lattice;
-    if (l[0] <= 0 || l[1] <= 0 || l[2] <= 0 || l[3] <= 0 || (l[0] & 1)) {
-      invalid("batch item %d: invalid lattice {%d, %d, %d, %d}", i, l[0], l[1], l[2], l[3]);
-      return;
-    }
-    const size_t v = (size_t)l[0] * l[1] * l[2] * l[3];
-    if (!ptr_ok(it.correl, v, "correl") || !ptr_ok(it.propag_i, v, "propag_i") ||
-        !ptr_ok(it.propag_j, v, "propag_j") || !ptr_ok(it.propag_n, v, "propag_n"))
-      return;
-    specs[i].in[0] = it.propag_i;
-    specs[i].in[1] = it.propag_j;
-    specs[i].in[2] = it.propag_n;
-    specs[i].out = static_cast<double2 *>(it.correl);
-    for (int k = 0; k < 4; ++k) specs[i].latt[k] = l[k];
-  }
+  BaryonBatch bb;
+  if (!baryon_batch_setup(bb, items, nitems, gamma_ij, gamma_kl, nproj, projectors, precision)) return;
   cgb::Job job;
   DevState *s = nullptr;
   if (!make_job(job, precision, 0, nullptr, &s)) return;
   DeviceWorkspace ws(s);
   job.ws = &ws;
-  OpParams<double> p {};
-  set_row(p.b.perm1, kG.perm[gamma_ij]);
-  set_row(p.b.perm2, kG.perm[gamma_kl]);
-  set_row(p.b.ph1[0], kG.ph[gamma_ij]);
-  set_row(p.b.ph1[1], kG.ph_t[gamma_ij]);
-  set_row(p.b.ph2[0], kG.ph_t[gamma_kl]);
-  set_row(p.b.ph2[1], kG.ph[gamma_kl]);
-  const double *pr = static_cast<const double *>(projectors);
-  const double *pw[2] = {pr, pr + 32};
-  for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
-  fill_clifford(p.b.cl, pw, nproj, 0);
-  if (p.b.cl.ng > nproj) {
-    invalid("batched contractions need projectors spanned by at most nproj gamma matrices (got %d terms)", p.b.cl.ng);
-    return;
-  }
-  cuda_ok(cgb::launch_baryon_fused_batch(job, nproj, p, specs.data(), nitems), "contract_baryon_all_types_batch");
+  cuda_ok(cgb::launch_baryon_fused_batch(job, nproj, bb.p, bb.specs.data(), nitems), "contract_baryon_all_types_batch");
+}
+
+void contract_meson_all_gamma_momentum_batch(const ContractMesonMomentumBatchItem *items, int nitems,
+                                             const int *moms, int nmom, int precision)
+{
+  run_mixed_batch(nullptr, 0, 0, 0, 1, nullptr, items, nitems, moms, nmom, precision,
+                  "contract_meson_all_gamma_momentum_batch");
+}
+
+void contract_batch_mixed(const ContractBaryonBatchItem *baryon_items, int nbaryon, int gamma_ij, int gamma_kl,
+                          int nproj, const void *projectors, const ContractMesonMomentumBatchItem *meson_items,
+                          int nmeson, const int *moms, int nmom, int precision)
+{
+  run_mixed_batch(baryon_items, nbaryon, gamma_ij, gamma_kl, nproj, projectors, meson_items, nmeson, moms, nmom,
+                  precision, "contract_batch_mixed");
 }
 
 void contract_sequential_sink(void *propag_i, void *propag_j, void *propag_n, BaryonContractType contract_type,

@@ -11,8 +11,18 @@ struct BatchSpec {
   int latt[4];
 };
 
+struct BaryonFinParams;
+
 // All six baryon types x nw projectors (gamma-basis projectors only) for n
-// items in one persistent launch plus one finalisation launch.
-cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<double> &p, const BatchSpec *specs, int n);
+// items in one persistent launch plus one finalisation launch -- or, with
+// fin != nullptr, without it: fin then describes the partial sums for the
+// caller's combined finalisation (launch_batch_finalize).  job.variant picks
+// the tile shape (batch_variants; -1 the default).
+cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<double> &p, const BatchSpec *specs, int n,
+                                      BaryonFinParams *fin = nullptr);
+// Names of the batched launch's tile shapes (the one-pass form when every
+// item passes one field as P_i and P_j, and Gamma_ij allows it).
+int batch_variants(bool same_field, const char *const **names);
+bool batch_same_field(const OpParams<double> &p, const BatchSpec *specs, int n);
 
 } // namespace cgb

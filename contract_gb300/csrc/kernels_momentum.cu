@@ -351,6 +351,135 @@ cudaError_t launch_finalize(const Job &job, const typename Vec2<R>::type *planes
   return cudaGetLastError();
 }
 
+// ------------------------------------------------ batched finalisation --
+// One launch for what the batched site kernels leave: blocks [0, bf.total_blocks)
+// sum the baryon items' partials per (output, timeslice) in the order of
+// batch_finalize_kernel (kernels_batch.cu), 256 values a block; the blocks
+// after them take one (item, pair q, timeslice) each and do what
+// momentum_finalize<float, CNT, true> does for one call: the Z transform of
+// the item's planes with a compensated FP32 sum, then the product -> Gamma
+// pair map, FP64 out.  Phase tables come from the batch's per-extent tables
+// (the same FP32 values as the per-call path).
+template <int CNT>
+__global__ void __launch_bounds__(256) batch_finalize_combined(const __grid_constant__ MomBatchParams mp,
+                                                                const __grid_constant__ BaryonFinParams bf)
+{
+  const int g = threadIdx.x;
+  if ((int)blockIdx.x < bf.total_blocks) {
+    int lo = 0, hi = bf.n_items - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (bf.items[mid].blk_begin <= (int)blockIdx.x) lo = mid;
+      else hi = mid - 1;
+    }
+    const BaryonFinItem &it = bf.items[lo];
+    const int idx = ((int)blockIdx.x - it.blk_begin) * 256 + g;
+    if (idx >= bf.nout * it.lt || it.per_seg <= 0) return;
+    const int o = idx / it.lt, t = idx % it.lt;
+    double sx = 0.0, sy = 0.0;
+    for (int par = 0; par < 2; ++par) {
+      const double2 *row = it.partial + ((size_t)(par * it.lt + t) * it.per_seg) * bf.nout + o;
+      for (int c = 0; c < it.per_seg; ++c) {
+        const double2 v = row[(size_t)c * bf.nout];
+        sx += v.x;
+        sy += v.y;
+      }
+    }
+    it.out[(size_t)o * it.lt + t] = make_double2(sx, sy);
+    return;
+  }
+  const int b = (int)blockIdx.x - bf.total_blocks;
+  int lo = 0, hi = mp.n_items - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (mp.items[mid].fin_begin <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const MomBatchItem &it = mp.items[lo];
+  const int lz = it.latt[2], lt = it.latt[3];
+  const int local = b - it.fin_begin, q = local / lt, t = local - q * lt;
+  if (q >= mp.nq) return;  // block-uniform
+  __shared__ float cz[kMomMaxL], sz[kMomMaxL];
+  __shared__ float2 tp[CNT][2][272];
+  __shared__ uint8_t gperm[16][4], gph[16][4];
+  if (g < 64) {
+    gperm[g >> 2][g & 3] = kMomGamma.perm[g >> 2][g & 3];
+    gph[g >> 2][g & 3] = kMomGamma.ph_g5g_t[g >> 2][g & 3];
+  }
+  for (int k = g; k < lz; k += blockDim.x) {
+    cz[k] = mp.tab[it.tz][k].x;
+    sz[k] = mp.tab[it.tz][k].y;
+  }
+  __syncthreads();
+  const PairTerms terms = pair_terms(gperm, gph, g);
+  const int g0 = mp.q_g0[q], g1 = mp.q_g0[q + 1];
+  for (int base = g0; base < g1; base += CNT) {
+    const int cnt = min(CNT, g1 - base);
+    ChunkSum<float> ca[CNT], sa[CNT];
+    int kk[CNT], step[CNT];
+#pragma unroll
+    for (int k = 0; k < CNT; ++k) {
+      kk[k] = 0;
+      step[k] = k < cnt ? mp.gz_k[base + k] : 0;
+    }
+    constexpr int ZB = 4;  // plane loads in flight per thread
+    for (int z0 = 0; z0 < lz; z0 += ZB) {
+      float2 v[ZB];
+#pragma unroll
+      for (int u = 0; u < ZB; ++u)
+        if (z0 + u < lz) v[u] = it.planes[((size_t)(t * lz + z0 + u) * mp.nq + q) * 256 + g];
+#pragma unroll
+      for (int u = 0; u < ZB; ++u) {
+        if (z0 + u >= lz) break;
+#pragma unroll
+        for (int k = 0; k < CNT; ++k) {
+          if (k < cnt) {
+            zacc(ca[k], cz[kk[k]], v[u]);
+            zacc(sa[k], sz[kk[k]], v[u]);
+            if ((kk[k] += step[k]) >= lz) kk[k] -= lz;
+          }
+        }
+      }
+    }
+    __syncthreads();  // the previous pass's reads of tp are done
+#pragma unroll
+    for (int k = 0; k < CNT; ++k) {
+      if (k < cnt) {
+        const cx<float> c = ca[k].value_f32(), sn = sa[k].value_f32();
+        tp[k][0][g + (g >> 4)] = make_float2(c.x - sn.y, c.y + sn.x);
+        tp[k][1][g + (g >> 4)] = make_float2(c.x + sn.y, c.y - sn.x);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < CNT; ++k) {
+      if (k >= cnt) break;
+#pragma unroll
+      for (int sg = 0; sg < 2; ++sg) {
+        const int pm = sg ? mp.gz_minus[base + k] : mp.gz_plus[base + k];
+        if (pm < 0) continue;
+        const cx<float> o = pair_from_products(tp[k][sg], terms);
+        it.out[((size_t)pm * lt + t) * 256 + g] = make_double2(o.x, o.y);
+      }
+    }
+  }
+}
+
+cudaError_t launch_batch_finalize(const Job &job, const MomBatchParams &mp, const BaryonFinParams &bf)
+{
+  const long long blocks = (long long)bf.total_blocks + (mp.n_items > 0 ? mp.total_fin : 0);
+  if (blocks <= 0) return cudaSuccess;
+  int most = 1;  // Z groups of the pair with the most
+  for (int q = 0; q < mp.nq; ++q) most = std::max(most, mp.q_g0[q + 1] - mp.q_g0[q]);
+  const unsigned grid = (unsigned)blocks;
+  if (mp.n_items == 0 || most <= 1) batch_finalize_combined<1><<<grid, 256, 0, job.stream>>>(mp, bf);
+  else if (most <= 2) batch_finalize_combined<2><<<grid, 256, 0, job.stream>>>(mp, bf);
+  else if (most <= 3) batch_finalize_combined<3><<<grid, 256, 0, job.stream>>>(mp, bf);
+  else if (most <= 4) batch_finalize_combined<4><<<grid, 256, 0, job.stream>>>(mp, bf);
+  else batch_finalize_combined<8><<<grid, 256, 0, job.stream>>>(mp, bf);
+  return cudaGetLastError();
+}
+
 // CONTRACT_MOMENTUM_UNFUSED=1 selects the three-kernel mixed form (site
 // values through HBM), for comparison.
 static bool fused_disabled()
@@ -363,8 +492,8 @@ static bool fused_disabled()
 }
 
 static const char *const kMomFusedNames[] = {"fused.site8.xy8", "three-kernel", "fused.site16.xy8"};
-static const char *const kMomTcNames[] = {"tc.unit512", "tc.unit256", "tc.unit1024"};
-static const int kMomTcSteps[] = {512, 256, 1024};
+static const char *const kMomTcNames[] = {"tc.unit128", "tc.unit64", "tc.unit192"};
+static const int kMomTcSteps[] = {128, 64, 192};
 
 int momentum_variants(Prec prec, int aux, const char *const **names)
 {
@@ -394,7 +523,8 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   const int tcv = tensor_cores && job.variant >= 0 && job.variant < 3 ? job.variant : 0;
   const TcGeom tg = make_tc_geom(plan, kMomTcSteps[tcv]);
   const size_t a_bytes = (tc_phase_bytes(tg) + 255) / 256 * 256;
-  const size_t plane_bytes = tensor_cores ? a_bytes + tc_partial_bytes(tg)
+  const size_t tile_bytes = job.tc_tiles ? 0 : a_bytes;  // phase tiles kept by the caller, or in the workspace
+  const size_t plane_bytes = tensor_cores ? tile_bytes + tc_partial_bytes(tg)
                                           : (size_t)lt * lz * plan.nq * 256 * 2 * (job.prec == Prec::C128 ? 8 : 4);
   char *ws = static_cast<char *>(job.ws->get(c_bytes + plane_bytes));
   if (!ws) return cudaErrorMemoryAllocation;
@@ -416,8 +546,10 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   else e = run_field<MesonAllGammaM>(job, convert_params<float>(q));
   if (e != cudaSuccess) return e;
   if (tensor_cores) {
-    e = launch_momentum_tc(job, plan, tg, ws, reinterpret_cast<unsigned char *>(ws + c_bytes),
-                           reinterpret_cast<float *>(ws + c_bytes + a_bytes), out);
+    unsigned char *tiles = job.tc_tiles ? static_cast<unsigned char *>(job.tc_tiles)
+                                        : reinterpret_cast<unsigned char *>(ws + c_bytes);
+    e = launch_momentum_tc(job, plan, tg, ws, tiles, reinterpret_cast<float *>(ws + c_bytes + tile_bytes), out,
+                           job.tc_tiles != nullptr && job.tc_tiles_ready);
     if (e != cudaSuccess) return e;
     const long long nrows = (long long)plan.np * lt;
     const int grid = (int)std::min<long long>(nrows, (long long)job.num_sms * 8);

@@ -8,10 +8,13 @@
 //   A'[2p  ][2s] =  Re Phi   A'[2p  ][2s+1] = -Im Phi   ->  D'[2p  ][n] = Re D[p][n]
 //   A'[2p+1][2s] =  Im Phi   A'[2p+1][2s+1] =  Re Phi   ->  D'[2p+1][n] = Im D[p][n]
 //   B'[n][2s + c] = (Re C[s][n], Im C[s][n])[c]
-// Every operand value x is split into two bf16 terms, hi = bf16(x) and
-// lo = bf16(x - hi), and the product keeps hi*hi + hi*lo + lo*hi ("split
-// bf16, three products"); the tensor core accumulates in FP32 in tensor
-// memory.  A k-step is 8 sites (K = 16 of the real GEMM).
+// Every operand value x is split into three bf16 terms, hi = bf16(x),
+// mid = bf16(x - hi) and lo = bf16(x - hi - mid) (24 significant bits, an
+// FP32 value's), and the product keeps every term pair down to second order:
+// hi*hi + hi*mid + mid*hi + mid*mid + hi*lo + lo*hi ("split bf16, six
+// products"); the terms dropped are of order 2^-24 of the product.  The
+// tensor core accumulates in FP32 in tensor memory.  A k-step is 8 sites
+// (K = 16 of the real GEMM).
 //
 // Work: units (momentum group of 128, block of k-steps, t, pair half) are
 // dealt round-robin to persistent CTAs, so the CTAs running together share
@@ -19,14 +22,15 @@
 // Roles in a CTA (352 threads):
 //   warp 0     one bulk copy per k-step of the 8 sites x 128 pairs (8 KB) of
 //              the complex64 field, stored pair-half-major so that it is
-//              contiguous, into a 10-deep staging ring (HBM latency)
-//   warp 10    bulk copies of the 16 KB phase tile per k-step (both m-tiles,
-//              hi and lo, pre-tiled in global memory) into a 5-deep operand ring
-//   warp 1     allocates the 512 TMEM columns and issues the MMAs: three
+//              contiguous, into an 8-deep staging ring (HBM latency)
+//   warp 10    bulk copies of the 24 KB phase tile per k-step (both m-tiles,
+//              hi, mid and lo, pre-tiled in global memory) into a 4-deep
+//              operand ring
+//   warp 1     allocates the 512 TMEM columns and issues the MMAs: six
 //              M=128 (pairs), N=256 (momentum rows), K=16 MMAs per k-step
-//              (field hi x phase hi, field hi x phase lo, field lo x phase hi)
-//              into one of two accumulator buffers of 256 columns
-//   warps 2-9  convert the staged FP32 values into the bf16 hi/lo field tile
+//              (the six term pairs above) into one of two accumulator
+//              buffers of 256 columns
+//   warps 2-9  convert the staged FP32 values into the bf16 hi/mid/lo field tile
 //              of the operand ring (four groups of two warps, each taking every
 //              fourth k-step), and all eight drain each accumulator buffer
 //              (kTcFlush k-steps of MMAs) into FP32 registers (tcgen05.ld) a
@@ -45,25 +49,28 @@ namespace cgb {
 
 namespace {
 
-constexpr int kTcOpStages = 5;    // operand ring: phase tile + converted field tile
-constexpr int kTcStgStages = 10;  // staging ring: complex64 field rows (HBM latency)
-constexpr int kTcFlush = 8;       // k-steps per accumulator buffer
+constexpr int kTcOpStages = 4;    // operand ring: phase tile + converted field tile
+constexpr int kTcStgStages = 8;   // staging ring: complex64 field rows (HBM latency)
+constexpr int kTcFlush = 2;       // k-steps per accumulator window (see the MMA issuer)
 constexpr int kTcGroups = 4;      // converter groups of two warps, one k-step each in turn
 constexpr int kTcDrainLag = 3;    // k-steps converted past a window's end before draining it (< kTcOpStages)
 constexpr int kTcThreads = 352;   // 11 warps
 constexpr int kTcHeader = 1024;   // barriers, TMEM slot, abort flag
-constexpr int kTcABytes = 16384;  // phase tile: {hi, lo} x 256 rows x 16 bf16
-constexpr int kTcBBytes = 8192;   // field tile: {hi, lo} x 128 pairs x 16 bf16
+constexpr int kTcTerms = 3;       // bf16 terms per operand value
+constexpr int kTcABytes = kTcTerms * 8192;  // phase tile: {hi, mid, lo} x 256 rows x 16 bf16
+constexpr int kTcBBytes = kTcTerms * 4096;  // field tile: {hi, mid, lo} x 128 pairs x 16 bf16
 constexpr int kTcOpBytes = kTcABytes + kTcBBytes;
 constexpr int kTcStgBytes = 8192; // 8 sites x 128 pairs x complex64
 constexpr int kTcSmem = kTcHeader + kTcOpStages * kTcOpBytes + kTcStgStages * kTcStgBytes;
+static_assert(kTcSmem <= 232448, "tensor-core projection does not fit in shared memory");
+static_assert(kTcDrainLag < kTcOpStages, "a window is drained before its operand slots are reused");
 // D[pair][row] (+)= field[pair][k] * phase[row][k]: M = 128 pairs, N = 256 rows.
 constexpr uint32_t kTcIdesc = umma_idesc_bf16(128, 256);
 constexpr uint32_t kTcLbo128 = 16 * 128, kTcLbo256 = 32 * 128, kTcSbo = 128;
 
 struct TcParams {
   const float2 *field;          // [Lt][2 pair halves][V3][128] complex64, lexicographic sites
-  const unsigned char *atiles;  // [MG][J][m-tile][hi, lo][4096 B]
+  const unsigned char *atiles;  // [MG][J][hi, mid, lo][256 rows x 16 bf16, core-matrix layout]
   float *partial;               // [U][128 pairs][256 momentum rows]
   DeviceStatus *status;
   TcGeom g;
@@ -89,13 +96,18 @@ __device__ __forceinline__ Unit decode(const TcGeom &g, int u)
 
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
 
-// (a, b) -> packed bf16 hi and lo terms (a in the low half).
-__device__ __forceinline__ void split2(float a, float b, uint32_t &hi, uint32_t &lo)
+// (a, b) -> packed bf16 hi, mid and lo terms (a in the low half); the
+// remainders a - hi and a - hi - mid are exact in FP32.
+__device__ __forceinline__ void split3(float a, float b, uint32_t &hi, uint32_t &mid, uint32_t &lo)
 {
   const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   const float2 hf = __bfloat1622float2(h);
+  const float ra = a - hf.x, rb = b - hf.y;
+  const __nv_bfloat162 m = __floats2bfloat162_rn(ra, rb);
+  const float2 mf = __bfloat1622float2(m);
   hi = bf16x2_bits(h);
-  lo = bf16x2_bits(__floats2bfloat162_rn(a - hf.x, b - hf.y));
+  mid = bf16x2_bits(m);
+  lo = bf16x2_bits(__floats2bfloat162_rn(ra - mf.x, rb - mf.y));
 }
 
 __device__ __forceinline__ void tc_abort(volatile int *abort_flag, DeviceStatus *st, unsigned int where)
@@ -195,43 +207,63 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
-    uint32_t gi = 0, win = 0, buf = 0;
+    // A window is kTcFlush k-steps into one accumulator buffer.  Its MMAs run
+    // small terms first: the five second-order term pairs of every k-step of
+    // the window, then the hi x hi products.  The tensor core's FP32
+    // accumulation truncates toward zero relative to the accumulator, so the
+    // small terms accumulate while it is small and only kTcFlush truncations
+    // fall at the scale of the window's sum.
+    uint32_t gi = 0, win = 0;
     bool ok = true;
     const uint32_t sbase = smem_addr(ops);
     for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
       const Unit w = decode(g, u);
       const int n = w.j1 - w.j0;
-      for (int i = 0; i < n; ++i, ++gi) {
-        const int s = gi % kTcOpStages;
-        const bool wf = (i % kTcFlush) == 0, wl = (i % kTcFlush) == kTcFlush - 1 || i == n - 1;
-        bool okw = true;
-        if (wf) {
-          buf = win & 1;
-          if (win >= 2) okw = mbar_wait_bounded(&acc_empty[buf], ((win >> 1) - 1) & 1, kWaitLimitNs);
+      for (int i0 = 0; i0 < n && ok; i0 += kTcFlush) {
+        const int nw = min(kTcFlush, n - i0);
+        const uint32_t buf = win & 1, d = tmem + buf * 256;
+        bool okw = win < 2 || mbar_wait_bounded(&acc_empty[buf], ((win >> 1) - 1) & 1, kWaitLimitNs);
+        for (int i = 0; i < nw; ++i) {
+          const uint32_t gk = gi + i;
+          const int s = gk % kTcOpStages;
+          okw = okw && mbar_wait_bounded(&a_full[s], (gk / kTcOpStages) & 1, kWaitLimitNs);
+          okw = okw && mbar_wait_bounded(&op_full[s], (gk / kTcOpStages) & 1, kWaitLimitNs);
+          ok = __all_sync(0xffffffffu, okw) && !*abort_flag;
+          if (!ok) {
+            if (lane == 0) tc_abort(abort_flag, p.status, 0x200000u | (unsigned)u);
+            break;
+          }
+          tc_fence_after();
+          if (lane == 0) {
+            const uint32_t st = sbase + s * kTcOpBytes;
+            const uint64_t ph = umma_desc(st, kTcLbo256, kTcSbo);              // phase tile, hi
+            const uint64_t pm = umma_desc(st + 8192, kTcLbo256, kTcSbo);       // phase tile, mid
+            const uint64_t pl = umma_desc(st + 2 * 8192, kTcLbo256, kTcSbo);   // phase tile, lo
+            const uint64_t fh = umma_desc(st + kTcABytes, kTcLbo128, kTcSbo);  // field tile, hi
+            const uint64_t fm = umma_desc(st + kTcABytes + 4096, kTcLbo128, kTcSbo);
+            const uint64_t fl = umma_desc(st + kTcABytes + 2 * 4096, kTcLbo128, kTcSbo);
+            umma_bf16(d, fh, pm, kTcIdesc, i == 0 ? 0u : 1u);
+            umma_bf16(d, fm, ph, kTcIdesc, 1u);
+            umma_bf16(d, fm, pm, kTcIdesc, 1u);
+            umma_bf16(d, fh, pl, kTcIdesc, 1u);
+            umma_bf16(d, fl, ph, kTcIdesc, 1u);
+          }
+          __syncwarp();
         }
-        okw = okw && mbar_wait_bounded(&a_full[s], (gi / kTcOpStages) & 1, kWaitLimitNs);
-        okw = okw && mbar_wait_bounded(&op_full[s], (gi / kTcOpStages) & 1, kWaitLimitNs);
-        ok = __all_sync(0xffffffffu, okw) && !*abort_flag;
-        if (!ok) {
-          if (lane == 0) tc_abort(abort_flag, p.status, 0x200000u | (unsigned)u);
-          break;
-        }
-        tc_fence_after();
+        if (!ok) break;
         if (lane == 0) {
-          const uint32_t st = sbase + s * kTcOpBytes;
-          const uint64_t ph = umma_desc(st, kTcLbo256, kTcSbo);         // phase tile, hi
-          const uint64_t pl = umma_desc(st + 8192, kTcLbo256, kTcSbo);  // phase tile, lo
-          const uint64_t fh = umma_desc(st + kTcABytes, kTcLbo128, kTcSbo);
-          const uint64_t fl = umma_desc(st + kTcABytes + 4096, kTcLbo128, kTcSbo);
-          const uint32_t d = tmem + buf * 256;
-          umma_bf16(d, fh, ph, kTcIdesc, wf ? 0u : 1u);
-          umma_bf16(d, fh, pl, kTcIdesc, 1u);
-          umma_bf16(d, fl, ph, kTcIdesc, 1u);
-          umma_commit(&op_empty[s]);
-          if (wl) umma_commit(&acc_full[buf]);
+          for (int i = 0; i < nw; ++i) {
+            const int s = (gi + i) % kTcOpStages;
+            const uint32_t st = sbase + s * kTcOpBytes;
+            umma_bf16(d, umma_desc(st + kTcABytes, kTcLbo128, kTcSbo), umma_desc(st, kTcLbo256, kTcSbo), kTcIdesc,
+                      1u);
+            umma_commit(&op_empty[s]);  // the k-step's operands are free once its MMAs complete
+          }
+          umma_commit(&acc_full[buf]);
         }
         __syncwarp();
-        if (wl) ++win;
+        gi += nw;
+        ++win;
       }
     }
     // every MMA issued by this CTA completes before TMEM is released
@@ -319,17 +351,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
             const int pair = t64 + 64 * pp;
 #pragma unroll
             for (int sh = 0; sh < 2; ++sh) {
-              uint32_t hi[4], lo[4];
+              uint32_t hi[4], mid[4], lo[4];
 #pragma unroll
               for (int k = 0; k < 4; ++k) {
                 const int s8 = sh * 4 + k;
                 float2 c = make_float2(0.f, 0.f);
                 if (s0 + s8 < g.v3) c = reinterpret_cast<const float2 *>(stg + s8 * 1024)[pair];
-                split2(c.x, c.y, hi[k], lo[k]);
+                split3(c.x, c.y, hi[k], mid[k], lo[k]);
               }
               const uint32_t off = (sh * 16 + (pair >> 3)) * 128 + (pair & 7) * 16;
               *reinterpret_cast<uint4 *>(bt + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-              *reinterpret_cast<uint4 *>(bt + 4096 + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+              *reinterpret_cast<uint4 *>(bt + 4096 + off) = make_uint4(mid[0], mid[1], mid[2], mid[3]);
+              *reinterpret_cast<uint4 *>(bt + 2 * 4096 + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
             }
           }
           fence_proxy_async_smem();
@@ -382,8 +415,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) momentum_gemm_tc(const __grid_c
 }
 
 // Phase tiles: for momentum group mg and k-step j, the two 128-row m-tiles
-// (64 momenta x {Re, Im} rows each) over the 8 sites of the step, bf16 hi and
-// lo, in the K-major core-matrix layout.  Phi = ex * ey * ez in FP64 from the
+// (64 momenta x {Re, Im} rows each) over the 8 sites of the step, bf16 hi,
+// mid and lo, in the K-major core-matrix layout.  Phi = ex * ey * ez in FP64 from the
 // FP64 tables exp(2 pi i k / L), k = (n * x) mod L exactly.
 __global__ void __launch_bounds__(256) momentum_phase_tiles(unsigned char *__restrict__ atiles,
                                                             const __grid_constant__ MomPlan plan, long long v3, int nj)
@@ -410,7 +443,7 @@ __global__ void __launch_bounds__(256) momentum_phase_tiles(unsigned char *__res
     ny = plan.q_ny[qq];
     nz = plan.p_nz[pm];
   }
-  uint32_t w[2][2][4];
+  uint32_t w[2][kTcTerms][4];
   // site coordinates and phase indices k = (n * x) mod L, advanced site by site
   const long long s_first = (long long)j * 8;
   int x = (int)(s_first % lx), y = (int)((s_first / lx) % ly), z = (int)(s_first / ((long long)lx * ly));
@@ -443,20 +476,27 @@ __global__ void __launch_bounds__(256) momentum_phase_tiles(unsigned char *__res
       kx -= lx;
     }
     const double a0 = comp ? im : re, a1 = comp ? re : -im;  // columns 2s (Re C) and 2s+1 (Im C)
-    const __nv_bfloat162 h = __floats2bfloat162_rn((float)a0, (float)a1);
-    const float2 hf = __bfloat1622float2(h);
-    const __nv_bfloat162 l = __floats2bfloat162_rn((float)(a0 - (double)hf.x), (float)(a1 - (double)hf.y));
-    w[s8 >> 2][0][s8 & 3] = bf16x2_bits(h);
-    w[s8 >> 2][1][s8 & 3] = bf16x2_bits(l);
+    // three bf16 terms, each the rounded FP64 remainder of the ones before
+    double r0 = a0, r1 = a1;
+#pragma unroll
+    for (int tm = 0; tm < kTcTerms; ++tm) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn((float)r0, (float)r1);
+      const float2 hf = __bfloat1622float2(h);
+      w[s8 >> 2][tm][s8 & 3] = bf16x2_bits(h);
+      r0 -= (double)hf.x;
+      r1 -= (double)hf.y;
+    }
   }
-  // one 256-row tile per term (hi, lo): row mt * 128 + r
-  unsigned char *tile = atiles + ((size_t)mg * nj + j) * 16384;
+  // one 256-row tile per term (hi, mid, lo): row mt * 128 + r
+  unsigned char *tile = atiles + ((size_t)mg * nj + j) * kTcABytes;
   const int row = mt * 128 + r;
 #pragma unroll
   for (int kc = 0; kc < 2; ++kc) {
     const uint32_t off = (kc * 32 + (row >> 3)) * 128 + (row & 7) * 16;
-    *reinterpret_cast<uint4 *>(tile + off) = make_uint4(w[kc][0][0], w[kc][0][1], w[kc][0][2], w[kc][0][3]);
-    *reinterpret_cast<uint4 *>(tile + 8192 + off) = make_uint4(w[kc][1][0], w[kc][1][1], w[kc][1][2], w[kc][1][3]);
+#pragma unroll
+    for (int tm = 0; tm < kTcTerms; ++tm)
+      *reinterpret_cast<uint4 *>(tile + tm * 8192 + off) =
+        make_uint4(w[kc][tm][0], w[kc][tm][1], w[kc][tm][2], w[kc][tm][3]);
   }
 }
 
@@ -494,7 +534,7 @@ size_t tc_phase_bytes(const TcGeom &g) { return (size_t)g.mg * g.j * kTcABytes; 
 size_t tc_partial_bytes(const TcGeom &g) { return (size_t)g.units * 2 * 128 * 128 * sizeof(float); }
 
 cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom &g, const void *field,
-                               unsigned char *atiles, float *partial, void *out)
+                               unsigned char *atiles, float *partial, void *out, bool tiles_ready)
 {
   static bool attr_set[64] = {};
   int dev = 0;
@@ -505,9 +545,11 @@ cudaError_t launch_momentum_tc(const Job &job, const MomPlan &plan, const TcGeom
     if (e != cudaSuccess) return e;
     attr_set[dev] = true;
   }
-  momentum_phase_tiles<<<dim3(g.j, g.mg), 256, 0, job.stream>>>(atiles, plan, g.v3, g.j);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (!tiles_ready) {
+    momentum_phase_tiles<<<dim3(g.j, g.mg), 256, 0, job.stream>>>(atiles, plan, g.v3, g.j);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   TcParams tp;
   tp.field = static_cast<const float2 *>(field);
   tp.atiles = atiles;

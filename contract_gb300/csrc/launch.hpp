@@ -32,6 +32,10 @@ struct Job {
   int variant = -1;          // tile-shape variant (-1: the launcher's default)
   unsigned long long wait_ns = 0;  // mbarrier wait limit of the site engines (0: kWaitLimitNs)
   int withhold_chunk = -1;         // test hook of the site engines (TileGeom::withhold_chunk)
+  // Tensor-core momentum projection: a buffer the caller keeps for the phase
+  // tiles of one (lattice, momentum list), and whether it already holds them.
+  void *tc_tiles = nullptr;
+  bool tc_tiles_ready = false;
 };
 
 // Ops whose launchers offer several compiled tile shapes (consumer warps,
@@ -67,6 +71,12 @@ cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParam
 cudaError_t launch_convert(const Job &job, void *dst, const void *src, bool to_c64);
 // Propagator site order lexicographic <-> PyQUDA even/odd (site_bytes per site).
 cudaError_t launch_layout(const Job &job, void *dst, const void *src, const int *latt, bool to_eo, int site_bytes);
+// Propagator <-> twelve colour-spinor fields in QUDA's native order (stride:
+// the fields' checkerboard length in 16-byte chunks; entry_bytes 16 or 8).
+cudaError_t launch_quda_layout(const Job &job, void *prop, void *const *fields, long long stride, bool from_quda,
+                               int entry_bytes);
+// In place P -> U P U^dagger on the spin indices; u: host 4 x 4 complex128, row-major.
+cudaError_t launch_spin_rotation(const Job &job, void *prop, const double *u);
 // Address of this device's status word (a __device__ variable of the library).
 cudaError_t device_status_ptr(DeviceStatus **out);
 // Device address and size of the fixed scratch array used by the

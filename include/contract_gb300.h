@@ -127,6 +127,31 @@ void contract_convert_precision(void *dst, const void *src, size_t volume, int t
  * counterpart in the reference. */
 void contract_convert_layout(void *dst, const void *src, const int *lattice, int to_eo, int precision);
 
+/* Propagators as QUDA's solver leaves them on the device: twelve
+ * colour-spinor fields, one per source (spin k, colour d), field 3k + d, each
+ * in QUDA's native order [parity][chunk][stride][16 bytes], a chunk holding 16
+ * bytes of the site's spin-colour vector (complex entry 3s + c, sink spin s,
+ * sink colour c): one entry per chunk in complex128 (QUDA_FLOAT2_FIELD_ORDER),
+ * two in complex64 (QUDA_FLOAT4_FIELD_ORDER).  QUDA's checkerboard site index
+ * is the PyQUDA even/odd order's, so sites keep their index.  fields: HOST
+ * array of 12 device pointers; stride: checkerboard length of the fields in
+ * sites, >= volume/2 (0 = volume/2, no padding).  The pad sites of the fields
+ * are neither read nor written.  Bit-exact both ways.  The baryon_2pt.py
+ * example receives its propagators from PyQUDA's invert (baryon_2pt.py:63),
+ * which converts QUDA's fields on the host; these calls do it on the device.
+ * No counterpart in the reference. */
+void contract_convert_from_quda(void *propag, void *const *fields, const int *lattice, size_t stride, int precision);
+void contract_convert_to_quda(void *const *fields, const void *propag, const int *lattice, size_t stride,
+                              int precision);
+
+/* In place change of spin basis of `volume` propagator sites:
+ * P[s][k] -> sum U[s][s'] P[s'][k'] conj(U[k][k']) for every colour pair;
+ * rotation: HOST 4 x 4 complex128, row-major (e.g. the unitary that takes a
+ * solver's gamma basis to DeGrand-Rossi, the basis every contraction here
+ * assumes).  FP64 arithmetic for complex128, FP32 for complex64.  No
+ * counterpart in the reference. */
+void contract_rotate_spin_basis(void *propag, size_t volume, const void *rotation, int precision);
+
 /* ------------------------------------------------------ contractions --- */
 /* meson_two_point with a precision and optional per-timeslice output. */
 void contract_meson(void *correl, const void *propag_i, const void *propag_j, size_t volume, int gamma_ij,
@@ -205,6 +230,40 @@ typedef struct {
  * batch to the two-pass form.  The two forms agree to FP32 rounding. */
 void contract_baryon_all_types_batch(const ContractBaryonBatchItem *items, int nitems, int gamma_ij, int gamma_kl,
                                      int nproj, const void *projectors, int precision);
+
+/* One work item of a batched meson momentum projection: a (P_i, P_j) pair on
+ * its own lattice (extents may differ between items). */
+typedef struct {
+  const void *propag_i, *propag_j;  /* device, complex64 */
+  void *correl;                     /* device complex128 [nmom][Lt][256] */
+  int lattice[4];                   /* Lx, Ly, Lz, Lt (PyQUDA even/odd order) */
+} ContractMesonMomentumBatchItem;
+
+/* contract_meson_all_gamma_momentum (CONTRACT_C64) for up to 128 items with
+ * one momentum list: one persistent launch over every item's (t, z) planes
+ * and one finalisation launch.  The list must give every item's lattice the
+ * same structure of +n/-n groups (any list with 2|n| < L in each direction
+ * does; e.g. n in {-1, 0, 1}^3 on L >= 3); at most 8 distinct spatial
+ * extents.  When every item passes one field as propag_i and propag_j, the
+ * launch forms the Hermitian site products.  No host synchronisation after a
+ * warm-up call; the workspace holds every item's FP32 planes. */
+void contract_meson_all_gamma_momentum_batch(const ContractMesonMomentumBatchItem *items, int nitems,
+                                             const int *moms, int nmom, int precision);
+
+/* The batched baryon and meson workloads of one set of sources together
+ * (CONTRACT_C64): the baryon items' all-types contraction (as
+ * contract_baryon_all_types_batch) in one persistent launch, the meson items'
+ * momentum projection (as contract_meson_all_gamma_momentum_batch) in
+ * another, and a single finalisation launch for both -- three kernel launches
+ * for any number of items.  With autotuning enabled, each launch's tile
+ * shape is chosen per lattice extent: every extent class is timed alone, and
+ * the launch takes the shape with the least total over its items (reported
+ * by contract_autotune_report per class and per batch).  Either count may be
+ * 0.  No counterpart in the reference, whose callers issue one launch per
+ * contraction (include/kernel.cuh:173-183). */
+void contract_batch_mixed(const ContractBaryonBatchItem *baryon_items, int nbaryon, int gamma_ij, int gamma_kl,
+                          int nproj, const void *projectors, const ContractMesonMomentumBatchItem *meson_items,
+                          int nmeson, const int *moms, int nmom, int precision);
 
 /* All 16 x 16 meson correlators (C(x) of meson_two_point for every
  * (gamma_ij, gamma_kl)) projected to momenta, per timeslice:

@@ -177,3 +177,30 @@ def test_batch_validation_without_gpu(lib):
         lib.contract_clear_error()
     finally:
         lib.contract_set_error_mode(0)
+
+
+def test_quda_conversion_argument_checks(lib):
+    lib.contract_set_error_mode(1)
+    try:
+        lat = (ctypes.c_int * 4)(4, 2, 2, 4)
+        fields = (ctypes.c_void_p * 12)(*[0x100000 * (k + 1) for k in range(12)])
+        lib.contract_clear_error()
+        lib.contract_convert_from_quda(0x10000000, fields, lat, 15, 0)  # stride below V/2 = 16
+        assert lib.contract_last_error() == 1 and b"stride" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        lib.contract_convert_to_quda(None, 0x10000000, lat, 0, 0)
+        assert lib.contract_last_error() == 1 and b"fields is NULL" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        fields[3] = fields[2] + 256  # overlaps field 2 (each field is 2 x 12 x 16 x 16 bytes)
+        lib.contract_convert_from_quda(0x10000000, fields, lat, 0, 0)
+        assert lib.contract_last_error() == 1 and b"overlap" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        fields[3] = 0x100008  # misaligned
+        lib.contract_convert_to_quda(fields, 0x10000000, lat, 0, 1)
+        assert lib.contract_last_error() == 1 and b"16-byte aligned" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        lib.contract_rotate_spin_basis(0x10000000, 16, None, 0)
+        assert lib.contract_last_error() == 1 and b"rotation is NULL" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+    finally:
+        lib.contract_set_error_mode(0)
