@@ -484,6 +484,47 @@ def test_fused_variants_forced(tmp_path):
         assert err < TOL_C64_TIMESLICE, (name, case, err)
 
 
+def test_baryon_variants_forced(tmp_path):
+    """Every compiled tile-shape variant of the per-call complex64 baryon
+    two-point -- loop form; triangle form with a gamma projector; triangle form
+    with N' materialised, for (1 + g4)/2 and for a dense projector -- forced
+    through a tune cache, against the FP64 oracle.  Each case uses its own
+    lattice shape, so that each tune key fixes one variant."""
+    import ctypes
+    import json
+    import os
+    import subprocess
+    import sys
+    from contract_gb300 import _lib, build
+    build.build()
+    lib = _lib.lib()
+    cache = tmp_path / "tune.txt"
+    lines, cases, names = [], [], []
+    for c, (op, aux, ctype, kind) in enumerate(((1, 0, 0, "g4"), (2, 0, 1, "g4"), (2, 1, 4, "pp"), (2, 1, 3, "dense"))):
+        buf = ctypes.create_string_buffer(4096)
+        n = lib.contract_variant_names(op, 1, aux, buf, len(buf))
+        vnames = buf.value.decode().split()
+        assert n == len(vnames) >= 4, (op, aux, vnames)
+        for v, name in enumerate(vnames):
+            latt = (4, 2 + 2 * c, 2, 3 + v)  # one lattice shape per (case, variant)
+            vol = int(np.prod(latt))
+            key = f"kind={op},prec=1,aux={aux},volume={vol},lt={latt[3]},half={vol // latt[3] // 2}"
+            lines.append(f"{key}\t{v} {name} 1.0\n")
+            cases.append([list(latt), ctype, kind])
+            names.append((op, aux, name))
+    cache.write_text("".join(lines))
+    env = dict(os.environ, CONTRACT_TUNE_CACHE=str(cache), CONTRACT_AUTOTUNE="0")
+    child = os.path.join(os.path.dirname(os.path.abspath(__file__)), "baryon_variants_child.py")
+    res = subprocess.run([sys.executable, child, json.dumps(cases)], env=env, capture_output=True, text=True,
+                         timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    out = json.loads(res.stdout.strip().splitlines()[-1])
+    for (_, _, name) in set(names):
+        assert name in out["report"], (name, out["report"])
+    for name, case, err in zip(names, cases, out["errors"]):
+        assert err < TOL_C64_TIMESLICE, (name, case, err)
+
+
 def test_momentum_variants_forced(tmp_path):
     """Each tile-shape variant of the momentum projection, forced through a tune
     cache: tensor-core work units of 192 k-steps (six units per timeslice on
