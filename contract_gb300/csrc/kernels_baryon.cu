@@ -16,19 +16,16 @@ static const VariantSet<float, 4> kLoopM = {
   {"cw7.tps16.st2", "cw5.tps16.st3", "cw4.tps8.st3", "cw3.tps16.st3"},
   0};
 // General projector (N' materialised per site).
-static const VariantSet<float, 6> kTriM = {
+static const VariantSet<float, 4> kTriM = {
   {run_scalar<BaryonTriOp<float, float2, 6, 16, 2>>, run_scalar<BaryonTriOp<float, float2, 7, 16, 3>>,
-   run_scalar<BaryonTriOp<float, float2, 4, 16, 3>>, run_scalar<BaryonTriOp<float, float2, 3, 16, 2>>,
-   run_scalar<BaryonTriOp<float, float2, 3, 16, 3>>, run_scalar<BaryonTriOp<float, float2, 2, 16, 3>>},
-  {"cw6.tps16.st2", "cw7.tps16.st3", "cw4.tps16.st3", "cw3.tps16.st2", "cw3.tps16.st3", "cw2.tps16.st3"},
+   run_scalar<BaryonTriOp<float, float2, 4, 16, 3>>, run_scalar<BaryonTriOp<float, float2, 3, 16, 2>>},
+  {"cw6.tps16.st2", "cw7.tps16.st3", "cw4.tps16.st3", "cw3.tps16.st2"},
   0};
-static const VariantSet<float, 7> kTriCliffM = {
+static const VariantSet<float, 5> kTriCliffM = {
   {run_scalar<BaryonTriCliffOp<float, float2, 7, 16, 2>>, run_scalar<BaryonTriCliffOp<float, float2, 5, 16, 3>>,
    run_scalar<BaryonTriCliffOp<float, float2, 4, 8, 2>>, run_scalar<BaryonTriCliffOp<float, float2, 3, 16, 2>>,
-   run_scalar<BaryonTriCliffOp<float, float2, 4, 16, 3>>, run_scalar<BaryonTriCliffOp<float, float2, 3, 16, 3>>,
-   run_scalar<BaryonTriCliffOp<float, float2, 2, 16, 3>>},
-  {"cw7.tps16.st2", "cw5.tps16.st3", "cw4.tps8.st2", "cw3.tps16.st2", "cw4.tps16.st3", "cw3.tps16.st3",
-   "cw2.tps16.st3"},
+   run_scalar<BaryonTriCliffOp<float, float2, 4, 16, 3>>},
+  {"cw7.tps16.st2", "cw5.tps16.st3", "cw4.tps8.st2", "cw3.tps16.st2", "cw4.tps16.st3"},
   0};
 
 cudaError_t launch_baryon(const Job &job, bool loop, const OpParams<double> &p)

@@ -204,3 +204,44 @@ def test_quda_conversion_argument_checks(lib):
         lib.contract_clear_error()
     finally:
         lib.contract_set_error_mode(0)
+
+
+class _MesonItem(ctypes.Structure):
+    _fields_ = [("propag_i", ctypes.c_void_p), ("propag_j", ctypes.c_void_p), ("correl", ctypes.c_void_p),
+                ("lattice", ctypes.c_int * 4)]
+
+
+def test_mixed_batch_validation_without_gpu(lib):
+    """The batched meson / mixed calls reject bad arguments on the host, before any
+    CUDA call (the pointers here are never dereferenced)."""
+    moms = np.array([[2, 0, 0], [-2, 0, 0], [0, 0, 0]], dtype=np.int32)
+    mp = moms.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    items = (_MesonItem * 2)()
+    for k, latt in enumerate(((4, 4, 4, 4), (6, 4, 4, 4))):
+        items[k].propag_i = items[k].propag_j = 0x100000 * (k + 1)
+        items[k].correl = 0x1000000 * (k + 1)
+        items[k].lattice = (ctypes.c_int * 4)(*latt)
+    lib.contract_set_error_mode(1)
+    try:
+        lib.contract_clear_error()
+        lib.contract_meson_all_gamma_momentum_batch(items, 2, mp, 3, 0)
+        assert lib.contract_last_error() == 1 and b"CONTRACT_C64" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        lib.contract_batch_mixed(None, 0, 5, 5, 2, None, items, 200, mp, 3, 1)
+        assert lib.contract_last_error() == 1 and b"item counts" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        # n = +-2 form one group on L = 4 and two on L = 6
+        lib.contract_meson_all_gamma_momentum_batch(items, 2, mp, 3, 1)
+        assert lib.contract_last_error() == 1 and b"another structure" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        items[1].lattice = (ctypes.c_int * 4)(66, 4, 4, 4)
+        lib.contract_meson_all_gamma_momentum_batch(items, 2, mp, 3, 1)
+        assert lib.contract_last_error() == 1 and b"up to 64" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+        items[1].propag_i = 0x100008  # misaligned
+        items[1].lattice = (ctypes.c_int * 4)(4, 4, 4, 4)
+        lib.contract_meson_all_gamma_momentum_batch(items, 2, mp, 3, 1)
+        assert lib.contract_last_error() == 1 and b"16-byte aligned" in lib.contract_last_error_message()
+        lib.contract_clear_error()
+    finally:
+        lib.contract_set_error_mode(0)
