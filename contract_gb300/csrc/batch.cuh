@@ -2,16 +2,20 @@
 //
 // A batch is up to kMaxBatch work items -- one per (source position,
 // propagator triple, lattice) -- that share one op and its spin tables.  The
-// queue travels as a kernel parameter (so it is captured by value in a CUDA
-// graph).  Each item's chunks are laid end to end in one global chunk space;
-// persistent CTAs deal global chunks round-robin exactly as the single-item
-// engine does, and for every chunk look up its item (binary search on
-// chunk_begin) for the geometry, the input pointers and the partial-sum
-// buffer.  Lattices of different extents therefore run in one launch.
+// items travel as a kernel parameter (so a CUDA graph captures them by
+// value).  Each item's chunks are laid end to end in one global chunk space,
+// and the queue is a counter in device memory over that space (zeroed by the
+// host before every launch): each CTA's producer warp takes the next chunk
+// with an atomic add whenever it has room in its ring, so CTAs that finish
+// early take more chunks and items of very different sizes balance without a
+// static schedule.  The producer looks up the chunk's item (binary search on
+// chunk_begin) for its geometry, inputs and partial-sum buffer, and hands
+// every tile to the consumer warps through a descriptor in shared memory
+// beside the ring stage; a final descriptor tells them the queue is empty.
 //
-// Every descriptor is validated on the device before use (extents, chunk
-// ranges, 16-byte alignment); a bad item is skipped and reported through the
-// status word as kDevErrBadWork.
+// Every item is validated on the device before use (extents, chunk ranges,
+// 16-byte alignment); a chunk of a bad item is skipped and reported through
+// the status word as kDevErrBadWork.
 #pragma once
 
 #include "ops.cuh"
@@ -32,10 +36,21 @@ struct BatchItem {
 template <class R> struct BatchParams {
   OpParams<R> op;  // spin tables; op.in/op.out unused
   DeviceStatus *status;
+  unsigned int *queue;  // next global chunk (zero at launch)
   int n_items;
   int total_chunks;
   BatchItem items[kMaxBatch];
 };
+
+// One tile as the producer hands it to the consumers.
+struct TileDesc {
+  long long first;  // first site of the tile in its item's volume
+  int item;         // work item
+  int local;        // chunk within the item
+  int n;            // sites in the tile
+  int flags;        // kTileLast: last tile of its chunk; kQueueEmpty: no more tiles
+};
+constexpr int kTileLast = 1, kQueueEmpty = 2;
 
 // Structural checks of one descriptor (identical in producer and consumers).
 template <int SITES, int NIN> __device__ __forceinline__ bool item_ok(const BatchItem &it)
@@ -82,12 +97,6 @@ template <int SITES, int NIN> struct BatchIter {
       ok = ntiles > 0;
     }
   }
-  template <class P> __device__ __forceinline__ bool valid(const P &p) const { return chunk < p.total_chunks; }
-  __device__ __forceinline__ bool last_in_chunk() const { return k == ntiles - 1; }
-  template <class P> __device__ __forceinline__ void next(const P &p)
-  {
-    if (!ok || ++k >= ntiles) set_chunk(p, chunk + gridDim.x);
-  }
   template <class P> __device__ __forceinline__ void sites(const P &p, long long &first, int &n) const
   {
     const TileGeom &g = p.items[item].geom;
@@ -101,44 +110,62 @@ template <int SITES, int NIN> struct BatchIter {
 
 template <class Op>
 __device__ __forceinline__ void produce_batch(const BatchParams<typename Op::R> &p, unsigned char *smem, uint64_t *full,
-                                              uint64_t *empty, volatile int *abort_flag)
+                                              uint64_t *empty, TileDesc *desc, volatile int *abort_flag)
 {
   using L = SiteLayout<typename Op::S>;
   constexpr int NST = Op::NST, NIN = Op::NIN, SITES = Op::SITES;
   const int lane = threadIdx.x & 31;
-  BatchIter<SITES, NIN> it;
-  it.set_chunk(p, blockIdx.x);
-  for (int u = 0; it.valid(p);) {
-    if (!it.ok) {  // a rejected descriptor: reported by the consumers, no tiles
-      it.next(p);
-      continue;
-    }
-    const int stage = u % NST;
+  // Wait (bounded) until ring slot u is free again; false after a timeout or abort.
+  auto slot_free = [&](int u) -> bool {
     if (u >= NST) {
-      const bool ok = mbar_wait_bounded_backoff(&empty[stage], ((u / NST) - 1) & 1, kWaitLimitNs, kProducerSleepNs);
+      const bool ok = mbar_wait_bounded_backoff(&empty[u % NST], ((u / NST) - 1) & 1, kWaitLimitNs, kProducerSleepNs);
       if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) {
           *abort_flag = 1;
-          report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
+          report(p.status, kDevErrWaitTimeout, (unsigned int)u);
         }
-        return;
+        return false;
       }
     }
-    if (*abort_flag) return;
-    long long first;
-    int n;
-    it.sites(p, first, n);
-    const BatchItem &item = p.items[it.item];
-    if (lane == 0) mbar_arrive_expect_tx(&full[stage], (uint32_t)n * NIN * L::SITE_BYTES);
-    __syncwarp();
-    unsigned char *dst = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
-    for (int c = lane; c < n * NIN; c += 32) {
-      const int q = c / n, s = c - q * n;
-      bulk_g2s(dst + ((size_t)q * SITES + s) * L::SLOT,
-               static_cast<const char *>(item.in[q]) + (first + s) * L::SITE_BYTES, L::SITE_BYTES, &full[stage]);
+    return !*abort_flag;
+  };
+  int u = 0;
+  for (;;) {
+    unsigned int c = 0;
+    if (lane == 0) c = atomicAdd(p.queue, 1u);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= (unsigned int)p.total_chunks) break;
+    BatchIter<SITES, NIN> it;
+    it.set_chunk(p, (int)c);
+    if (!it.ok) {  // a rejected item: its chunks are skipped
+      if (lane == 0) report(p.status, kDevErrBadWork, c);
+      continue;
     }
-    ++u;
-    it.next(p);
+    for (; it.k < it.ntiles; ++it.k, ++u) {
+      if (!slot_free(u)) return;
+      const int stage = u % NST;
+      long long first;
+      int n;
+      it.sites(p, first, n);
+      const BatchItem &item = p.items[it.item];
+      if (lane == 0) {
+        desc[stage] = TileDesc {first, it.item, it.local, n, it.k == it.ntiles - 1 ? kTileLast : 0};
+        mbar_arrive_expect_tx(&full[stage], (uint32_t)n * NIN * L::SITE_BYTES);
+      }
+      __syncwarp();
+      unsigned char *dst = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
+      for (int q0 = lane; q0 < n * NIN; q0 += 32) {
+        const int q = q0 / n, s = q0 - q * n;
+        bulk_g2s(dst + ((size_t)q * SITES + s) * L::SLOT,
+                 static_cast<const char *>(item.in[q]) + (first + s) * L::SITE_BYTES, L::SITE_BYTES, &full[stage]);
+      }
+    }
+  }
+  // the queue is empty: one more slot tells the consumers so
+  if (!slot_free(u)) return;
+  if (lane == 0) {
+    desc[u % NST] = TileDesc {0, 0, 0, 0, kQueueEmpty};
+    mbar_arrive(&full[u % NST]);
   }
 }
 
@@ -154,6 +181,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_ke
 
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(16) typename Op::Params ps;
+  __shared__ TileDesc desc[NST];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   uint64_t *empty = full + NST;
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + 120);
@@ -169,7 +197,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_ke
   copy_params(ps, p.op);
   __syncthreads();
   if (warp == 0) {
-    produce_batch<Op>(p, smem, full, empty, abort_flag);
+    produce_batch<Op>(p, smem, full, empty, desc, abort_flag);
     return;
   }
 
@@ -180,34 +208,26 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_ke
   S *scratch = reinterpret_cast<S *>(smem + Smem<Op>::EXTRA + (size_t)site * Op::EXTRA_BYTES);
   ChunkSum<R> chunk_acc;
 
-  BatchIter<SITES, NIN> it;
-  it.set_chunk(p, blockIdx.x);
-  for (int u = 0; it.valid(p);) {
-    if (!it.ok) {
-      if (lane == 0 && w == 0) report(p.status, kDevErrBadWork, (unsigned int)it.chunk);
-      it.next(p);
-      continue;
-    }
+  for (int u = 0;; ++u) {
     const int stage = u % NST;
-    long long first;
-    int n;
-    it.sites(p, first, n);
     const bool ok = mbar_wait_bounded(&full[stage], (u / NST) & 1, kWaitLimitNs);
     if (!__all_sync(0xffffffffu, ok) || *abort_flag) {
       if (lane == 0) {
         *abort_flag = 1;
-        report(p.status, kDevErrWaitTimeout, (unsigned int)it.chunk);
+        report(p.status, kDevErrWaitTimeout, (unsigned int)u);
         drain<NST>(full, u, kWaitLimitNs);
       }
       return;
     }
+    const TileDesc d = desc[stage];  // read before the stage is released
+    if (d.flags & kQueueEmpty) return;
     const unsigned char *sb = smem + Smem<Op>::STAGES + stage * Smem<Op>::STAGE;
     const S *in[NIN];
 #pragma unroll
     for (int q = 0; q < NIN; ++q) in[q] = reinterpret_cast<const S *>(sb + ((size_t)q * SITES + site) * L::SLOT);
     cx<R> vals[NOUT];
     Op::site(ps, in, scratch, sub, vals);
-    const bool valid = site < n;
+    const bool valid = site < d.n;
     if constexpr (kScatterSums<TPS, NOUT>) {
       // many outputs: thread sub keeps the site sum of output sub
       const cx<R> mine = group_reduce_scatter<TPS, NOUT>(vals, sub);
@@ -228,14 +248,12 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_ke
     if (lane < NOUT) {
 #pragma unroll
       for (int s = 0; s < SPW; ++s) chunk_acc.add(sv[s * NOUT + lane]);
-      if (it.last_in_chunk()) {
-        p.items[it.item].partial[((size_t)it.local * CW + w) * NOUT + lane] = chunk_acc.value();
+      if (d.flags & kTileLast) {
+        p.items[d.item].partial[((size_t)d.local * CW + w) * NOUT + lane] = chunk_acc.value();
         chunk_acc.reset();
       }
     }
     __syncwarp();
-    ++u;
-    it.next(p);
   }
 }
 

@@ -46,8 +46,12 @@ static cudaError_t run_batch(const Job &job, const OpParams<typename Op::R> &op,
     max_lt = std::max<long long>(max_lt, ji.lt);
   }
   bp.total_chunks = chunks;
-  double2 *partial = static_cast<double2 *>(job.ws->get(partial_total * sizeof(double2)));
-  if (!partial) return cudaErrorMemoryAllocation;
+  // the partial sums, then the queue's counter
+  const size_t partial_bytes = (partial_total * sizeof(double2) + 255) / 256 * 256;
+  char *ws = static_cast<char *>(job.ws->get(partial_bytes + 256));
+  if (!ws) return cudaErrorMemoryAllocation;
+  double2 *partial = reinterpret_cast<double2 *>(ws);
+  bp.queue = reinterpret_cast<unsigned int *>(ws + partial_bytes);
   size_t off = 0;
   for (int i = 0; i < n; ++i) {
     bp.items[i].partial = partial + off;
@@ -58,6 +62,8 @@ static cudaError_t run_batch(const Job &job, const OpParams<typename Op::R> &op,
   cudaError_t e = prepare<Op>(batch_scalar_kernel<Op>, smem, bps);
   if (e != cudaSuccess) return e;
   const int grid = (int)std::min<long long>(chunks, (long long)job.num_sms * bps);
+  e = cudaMemsetAsync(bp.queue, 0, sizeof(unsigned int), job.stream);
+  if (e != cudaSuccess) return e;
   batch_scalar_kernel<Op><<<grid, Op::THREADS, smem, job.stream>>>(bp);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
