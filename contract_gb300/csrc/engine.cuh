@@ -166,7 +166,6 @@ template <> struct ChunkSum<float> {
     two_sum(hy, ly, v.y);
   }
   __device__ __forceinline__ double2 value() const { return make_double2((double)hx + (double)lx, (double)hy + (double)ly); }
-  __device__ __forceinline__ cx<float> value_f32() const { return {hx + lx, hy + ly}; }  // rounded to FP32
   __device__ __forceinline__ void reset() { hx = lx = hy = ly = 0.f; }
 };
 template <> struct ChunkSum<double> {

@@ -188,68 +188,127 @@ __device__ __forceinline__ void zacc(ChunkSum<float> &a, float c, float2 v) { a.
 
 //   TMAP (planes of the fused kernel, which projects the spin-colour products
 //     T[i][j][k][l] instead of the Gamma pairs): each momentum's 256 sums go
-//     through shared memory, rounded to FP32, and become the Gamma pairs
-//     (pair_from_products).
+//     through shared memory as unevaluated FP32 sums hi + lo (the compensated
+//     accumulator's two words) and become the Gamma pairs (map_pairs) with
+//     compensated sums again.  A Gamma pair is a signed sum of 16 products
+//     that can cancel to well below the products themselves (at zero momentum
+//     with one field in both slots the diagonal products are sums of positive
+//     values); rounding each product to FP32 before that sum would leave an
+//     error of the products' size.
 __constant__ GammaTables kMomGamma = build_gamma_tables();
 
-// Gamma pair (A, B) = g from the 256 projected products:
+// Gamma pair (A, B) from the 256 projected products:
 //   sum_{j,k} i^(ph_A(j) + ph_B(k)) T[perm_A(j)][j][k][perm_B(k)],
-// ph_n(r) the phase of (g5 Gamma(n)) at (r, perm_n(r)), in FP32 (its rounding
-// is of the order of the operands' own).  Products are staged at
-// index p + p / 16 (rows of 16 padded by one against bank conflicts);
-// pair_terms gives each term's staging index and phase.
-struct PairTerms {
-  int src[16];
-  uint32_t phs;  // 2 bits per term
-};
-__device__ __forceinline__ PairTerms pair_terms(const uint8_t (*gperm)[4], const uint8_t (*gph)[4], int g)
-{
-  PairTerms t;
-  t.phs = 0u;
-  const int A = g >> 4, B = g & 15;
-#pragma unroll
-  for (int jj = 0; jj < 4; ++jj) {
-    const int ia = gperm[A][jj];
-#pragma unroll
-    for (int kb = 0; kb < 4; ++kb) {
-      const int lb = gperm[B][kb];
-      t.src[jj * 4 + kb] = (kb * 4 + lb) * 17 + (ia ^ jj) * 4 + ia;
-      t.phs |= ((uint32_t)(gph[A][ia] + gph[B][lb]) & 3u) << (2 * (jj * 4 + kb));
+// ph_n(r) the phase of (g5 Gamma(n)) at (perm_n(r), r).  The phase factorises,
+// so the map runs in two stages of four terms each instead of one of sixteen:
+//   stage 1, thread 16 (4 i + j) + B:  U[i][j][B] = sum_k i^ph_B(k) T[i][j][k][perm_B(k)]
+//   stage 2, thread 16 A + B:          pair(A, B) = sum_j i^ph_A(j) U[perm_A(j)][j][B]
+// Products are staged at index p + p / 16 (rows of 16 padded by one against
+// bank conflicts), U at 16 (4 i + j) + B; high and low words in separate arrays.
+template <int NS> struct PairSmem {  // NS momenta mapped at a time
+  float2 th[NS][272], tl[NS][272];
+  float2 uh[NS][256], ul[NS][256];
+  uint8_t perm[16][4], ph[16][4];
+  __device__ __forceinline__ void load_tables(int g)
+  {
+    if (g < 64) {
+      perm[g >> 2][g & 3] = kMomGamma.perm[g >> 2][g & 3];
+      ph[g >> 2][g & 3] = kMomGamma.ph_g5g_t[g >> 2][g & 3];
     }
   }
-  return t;
-}
-__device__ __forceinline__ cx<float> pair_from_products(const float2 *staged, const PairTerms &t)
+};
+struct PairMap {
+  int s1[4], s2[4];  // each stage's source indices
+  uint32_t ph;       // 2-bit phases: stage 1 in bits 0-7, stage 2 in bits 8-15
+};
+template <int NS> __device__ __forceinline__ PairMap pair_map(const PairSmem<NS> &s, int g)
 {
-  cx<float> o = czero<float>();
+  PairMap m;
+  m.ph = 0u;
+  const int i = g >> 6, j = (g >> 4) & 3, A = g >> 4, B = g & 15;
 #pragma unroll
-  for (int e = 0; e < 16; ++e) {
-    const float2 v = staged[t.src[e]];
-    o = cadd(o, mul_phase(cx<float> {v.x, v.y}, (t.phs >> (2 * e)) & 3u));
+  for (int r = 0; r < 4; ++r) {
+    const int lb = s.perm[B][r], ia = s.perm[A][r];
+    m.s1[r] = (r * 4 + lb) * 17 + (i ^ j) * 4 + i;
+    m.s2[r] = (ia * 4 + r) * 16 + B;
+    m.ph |= ((uint32_t)s.ph[B][lb] & 3u) << (2 * r);
+    m.ph |= ((uint32_t)s.ph[A][ia] & 3u) << (8 + 2 * r);
   }
-  return o;
+  return m;
+}
+// One term hi + lo times i^ph (exact: a swap and sign flips); the high words
+// meet in a two-sum, the low words in a plain FP32 sum (they are of the order
+// of the high words' rounding).
+__device__ __forceinline__ void add_term(ChunkSum<float> &o, float2 h, float2 l, uint32_t ph)
+{
+  const cx<float> lp = mul_phase(cx<float> {l.x, l.y}, ph);
+  o.lx += lp.x;
+  o.ly += lp.y;
+  o.add(mul_phase(cx<float> {h.x, h.y}, ph));
+}
+// The Gamma pairs of the NS staged momenta, thread g's pair (A, B) = (g / 16,
+// g % 16) of each.  Call after a barrier that follows the staging; contains
+// one barrier (between the stages).
+template <int NS>
+__device__ __forceinline__ void map_pairs(PairSmem<NS> &s, const PairMap &m, int g, double2 (&out)[NS])
+{
+#pragma unroll
+  for (int n = 0; n < NS; ++n) {
+    ChunkSum<float> u;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) add_term(u, s.th[n][m.s1[r]], s.tl[n][m.s1[r]], (m.ph >> (2 * r)) & 3u);
+    s.uh[n][g] = make_float2(u.hx, u.hy);
+    s.ul[n][g] = make_float2(u.lx, u.ly);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int n = 0; n < NS; ++n) {
+    ChunkSum<float> o;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) add_term(o, s.uh[n][m.s2[r]], s.ul[n][m.s2[r]], (m.ph >> (8 + 2 * r)) & 3u);
+    out[n] = o.value();
+  }
+}
+
+// Stage the projected products of one Z group for momenta +n (n = 0) and -n
+// (n = 1) from the compensated cosine and sine sums: G(+-n) = C +- i S, the
+// high words joined by a two-sum.
+__device__ __forceinline__ void stage_products(const ChunkSum<float> &c, const ChunkSum<float> &s, int g,
+                                               PairSmem<2> &ps)
+{
+  const int slot = g + (g >> 4);
+#pragma unroll
+  for (int n = 0; n < 2; ++n) {
+    // +n: (C.re - S.im, C.im + S.re); -n: (C.re + S.im, C.im - S.re)
+    const float fx = n ? 1.f : -1.f, fy = -fx;
+    float hx = c.hx, lx = c.lx + fx * s.ly, hy = c.hy, ly = c.ly + fy * s.lx;
+    ChunkSum<float>::two_sum(hx, lx, fx * s.hy);
+    ChunkSum<float>::two_sum(hy, ly, fy * s.hx);
+    ps.th[n][slot] = make_float2(hx, hy);
+    ps.tl[n][slot] = make_float2(lx, ly);
+  }
 }
 
 // In place over rows of 256 (one (momentum, timeslice) each): projected
-// products -> Gamma pairs.  Used after the tensor-core projection of products.
+// products -> Gamma pairs.  Used after the tensor-core projection of products,
+// whose FP64 sums are split into FP32 words hi + lo for the staging.
 __global__ void __launch_bounds__(256) pair_map_kernel(double2 *__restrict__ rows, long long nrows)
 {
   const int g = threadIdx.x;
-  __shared__ float2 tp[272];
-  __shared__ uint8_t gperm[16][4], gph[16][4];
-  if (g < 64) {
-    gperm[g >> 2][g & 3] = kMomGamma.perm[g >> 2][g & 3];
-    gph[g >> 2][g & 3] = kMomGamma.ph_g5g_t[g >> 2][g & 3];
-  }
+  __shared__ PairSmem<1> ps;
+  ps.load_tables(g);
   __syncthreads();
-  const PairTerms terms = pair_terms(gperm, gph, g);
+  const PairMap m = pair_map(ps, g);
   for (long long r = blockIdx.x; r < nrows; r += gridDim.x) {
     const double2 v = rows[r * 256 + g];
-    __syncthreads();  // the previous row's reads of tp are done
-    tp[g + (g >> 4)] = make_float2(float(v.x), float(v.y));
+    __syncthreads();  // the previous row's reads of the staging are done
+    const float hx = float(v.x), hy = float(v.y);
+    ps.th[0][g + (g >> 4)] = make_float2(hx, hy);
+    ps.tl[0][g + (g >> 4)] = make_float2(float(v.x - hx), float(v.y - hy));
     __syncthreads();
-    const cx<float> o = pair_from_products(tp, terms);
-    rows[r * 256 + g] = make_double2(o.x, o.y);
+    double2 o[1];
+    map_pairs<1>(ps, m, g, o);
+    rows[r * 256 + g] = o[0];
   }
 }
 
@@ -260,14 +319,8 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
   const int q = blockIdx.x, t = blockIdx.y, g = threadIdx.x;
   const int lz = plan.latt[2], lt = plan.latt[3];
   __shared__ R cz[kMomMaxL], sz[kMomMaxL];
-  // TMAP staging: product index g at g + g / 16 (rows of 16 padded by one, so
-  // that a warp's gathers below fall in distinct banks)
-  __shared__ float2 tp[TMAP ? CNT : 1][2][272];
-  __shared__ uint8_t gperm[16][4], gph[16][4];
-  if (TMAP && g < 64) {
-    gperm[g >> 2][g & 3] = kMomGamma.perm[g >> 2][g & 3];
-    gph[g >> 2][g & 3] = kMomGamma.ph_g5g_t[g >> 2][g & 3];
-  }
+  __shared__ PairSmem<2> ps;  // TMAP: the pair map of one Z group (+n and -n)
+  if (TMAP) ps.load_tables(g);
   for (int k = g; k < lz; k += blockDim.x) {
     cz[k] = R(plan.cosz[k]);
     sz[k] = R(plan.sinz[k]);
@@ -303,35 +356,25 @@ __global__ void __launch_bounds__(256) momentum_finalize(const typename Vec2<R>:
         }
       }
     }
-    if constexpr (TMAP) __syncthreads();  // the previous pass's reads of tp are done
 #pragma unroll
     for (int k = 0; k < CNT; ++k) {
-      if (k < cnt) {
-        if constexpr (TMAP) {  // FP32 from here on: no FP64-pipe conversions
-          const cx<float> c = ca[k].value_f32(), sn = sa[k].value_f32();
-          tp[k][0][g + (g >> 4)] = make_float2(c.x - sn.y, c.y + sn.x);
-          tp[k][1][g + (g >> 4)] = make_float2(c.x + sn.y, c.y - sn.x);
-        } else {
-          const double2 c = ca[k].value(), sn = sa[k].value();
-          const int pp = plan.gz_plus[base + k], pn = plan.gz_minus[base + k];
-          if (pp >= 0) out[((size_t)pp * lt + t) * 256 + g] = make_double2(c.x - sn.y, c.y + sn.x);
-          if (pn >= 0) out[((size_t)pn * lt + t) * 256 + g] = make_double2(c.x + sn.y, c.y - sn.x);
-        }
-      }
-    }
-    if constexpr (TMAP) {
-      __syncthreads();
-      const PairTerms terms = pair_terms(gperm, gph, g);
-#pragma unroll
-      for (int k = 0; k < CNT; ++k) {
-        if (k >= cnt) break;
+      if (k >= cnt) break;  // block-uniform
+      if constexpr (TMAP) {
+        __syncthreads();  // the previous group's reads of the staging are done
+        stage_products(ca[k], sa[k], g, ps);
+        __syncthreads();
+        double2 o[2];
+        map_pairs<2>(ps, pair_map(ps, g), g, o);
 #pragma unroll
         for (int sg = 0; sg < 2; ++sg) {
           const int pm = sg ? plan.gz_minus[base + k] : plan.gz_plus[base + k];
-          if (pm < 0) continue;
-          const cx<float> o = pair_from_products(tp[k][sg], terms);
-          out[((size_t)pm * lt + t) * 256 + g] = make_double2(o.x, o.y);
+          if (pm >= 0) out[((size_t)pm * lt + t) * 256 + g] = o[sg];
         }
+      } else {
+        const double2 c = ca[k].value(), sn = sa[k].value();
+        const int pp = plan.gz_plus[base + k], pn = plan.gz_minus[base + k];
+        if (pp >= 0) out[((size_t)pp * lt + t) * 256 + g] = make_double2(c.x - sn.y, c.y + sn.x);
+        if (pn >= 0) out[((size_t)pn * lt + t) * 256 + g] = make_double2(c.x + sn.y, c.y - sn.x);
       }
     }
   }
@@ -400,18 +443,14 @@ __global__ void __launch_bounds__(256) batch_finalize_combined(const __grid_cons
   const int local = b - it.fin_begin, q = local / lt, t = local - q * lt;
   if (q >= mp.nq) return;  // block-uniform
   __shared__ float cz[kMomMaxL], sz[kMomMaxL];
-  __shared__ float2 tp[CNT][2][272];
-  __shared__ uint8_t gperm[16][4], gph[16][4];
-  if (g < 64) {
-    gperm[g >> 2][g & 3] = kMomGamma.perm[g >> 2][g & 3];
-    gph[g >> 2][g & 3] = kMomGamma.ph_g5g_t[g >> 2][g & 3];
-  }
+  __shared__ PairSmem<2> ps;
+  ps.load_tables(g);
   for (int k = g; k < lz; k += blockDim.x) {
     cz[k] = mp.tab[it.tz][k].x;
     sz[k] = mp.tab[it.tz][k].y;
   }
   __syncthreads();
-  const PairTerms terms = pair_terms(gperm, gph, g);
+  const PairMap pm_terms = pair_map(ps, g);
   const int g0 = mp.q_g0[q], g1 = mp.q_g0[q + 1];
   for (int base = g0; base < g1; base += CNT) {
     const int cnt = min(CNT, g1 - base);
@@ -441,25 +480,18 @@ __global__ void __launch_bounds__(256) batch_finalize_combined(const __grid_cons
         }
       }
     }
-    __syncthreads();  // the previous pass's reads of tp are done
 #pragma unroll
     for (int k = 0; k < CNT; ++k) {
-      if (k < cnt) {
-        const cx<float> c = ca[k].value_f32(), sn = sa[k].value_f32();
-        tp[k][0][g + (g >> 4)] = make_float2(c.x - sn.y, c.y + sn.x);
-        tp[k][1][g + (g >> 4)] = make_float2(c.x + sn.y, c.y - sn.x);
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < CNT; ++k) {
-      if (k >= cnt) break;
+      if (k >= cnt) break;  // block-uniform
+      __syncthreads();  // the previous group's reads of the staging are done
+      stage_products(ca[k], sa[k], g, ps);
+      __syncthreads();
+      double2 o[2];
+      map_pairs<2>(ps, pm_terms, g, o);
 #pragma unroll
       for (int sg = 0; sg < 2; ++sg) {
         const int pm = sg ? mp.gz_minus[base + k] : mp.gz_plus[base + k];
-        if (pm < 0) continue;
-        const cx<float> o = pair_from_products(tp[k][sg], terms);
-        it.out[((size_t)pm * lt + t) * 256 + g] = make_double2(o.x, o.y);
+        if (pm >= 0) it.out[((size_t)pm * lt + t) * 256 + g] = o[sg];
       }
     }
   }

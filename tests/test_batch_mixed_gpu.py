@@ -107,7 +107,7 @@ def check_meson_oracle(m, moms, got):
     sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, m["latt"]).real).T[None]
     l1 = eo.meson_product_l1(m["pi"], m["pj"], m["latt"]) if m["pi"] is m["pj"] else 0.0
     err = np.abs(got - ref) / np.maximum(np.maximum(np.abs(ref), sig), l1)
-    assert err.max() < (2e-6 if m["pi"] is m["pj"] else TOL_C64_TIMESLICE), (m["latt"], err.max())
+    assert err.max() < TOL_C64_TIMESLICE, (m["latt"], err.max())
 
 
 @pytest.mark.parametrize("same", [False, True])
