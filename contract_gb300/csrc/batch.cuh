@@ -112,7 +112,7 @@ template <class Op>
 __device__ __forceinline__ void produce_batch(const BatchParams<typename Op::R> &p, unsigned char *smem, uint64_t *full,
                                               uint64_t *empty, TileDesc *desc, volatile int *abort_flag)
 {
-  using L = SiteLayout<typename Op::S>;
+  using L = OpLayout<Op>;
   constexpr int NST = Op::NST, NIN = Op::NIN, SITES = Op::SITES;
   const int lane = threadIdx.x & 31;
   // Wait (bounded) until ring slot u is free again; false after a timeout or abort.
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) batch_scalar_ke
 {
   using S = typename Op::S;
   using R = typename Op::R;
-  using L = SiteLayout<S>;
+  using L = OpLayout<Op>;
   constexpr int NIN = Op::NIN, SITES = Op::SITES, TPS = Op::TPS, NST = Op::NST, NOUT = Op::NOUT;
   constexpr int SPW = 32 / TPS, CW = Op::CW;
 

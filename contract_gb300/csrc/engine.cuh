@@ -16,10 +16,11 @@
 // stage is free (`empty` mbarrier, one arrival per consumer warp), arms the
 // stage's `full` mbarrier with the tile's byte count and has its 32 lanes
 // issue the tile's cp.async.bulk (TMA) copies -- one per site and input, each
-// into its own padded shared-memory slot (+16 B, which staggers consecutive
-// sites across banks).  The CW consumer warps each own SPW = 32/TPS sites of
-// every tile; they wait on `full`, compute, and release the stage.  Warps
-// never meet at a CTA-wide barrier, so a slow warp only delays itself.
+// into its own padded shared-memory slot (+16 B, or the op's SLOT_PAD, which
+// staggers consecutive sites across banks).  The CW consumer warps each own
+// SPW = 32/TPS sites of every tile; they wait on `full`, compute, and release
+// the stage.  Warps never meet at a CTA-wide barrier, so a slow warp only
+// delays itself.
 //
 // Every wait is bounded in wall time.  A timed-out wait sets a bit in the
 // device status word and a CTA-local abort flag, waits (bounded again) for
@@ -36,6 +37,8 @@
 // lanes write it to a per-warp shared-memory staging slot (double-buffered)
 // and lane 0 stores it with cp.async.bulk shared->global copies.
 #pragma once
+
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -88,10 +91,22 @@ template <int SITES> struct TileIter {
   }
 };
 
-template <class S> struct SiteLayout {
+// One site's propagator in a ring stage: 144 complex values, then PAD bytes so
+// that consecutive sites start in different shared-memory banks (a multiple of
+// 16, as the bulk copies need).
+template <class S, int PAD = 16> struct SiteLayout {
   static constexpr uint32_t SITE_BYTES = 144 * sizeof(S);
-  static constexpr uint32_t SLOT = SITE_BYTES + 16;
+  static constexpr uint32_t SLOT = SITE_BYTES + PAD;
+  static_assert(SLOT % 16 == 0, "site slots must stay 16-byte aligned");
 };
+// An op's slot layout: its SLOT_PAD if it declares one, else 16 bytes.
+template <class Op, class = void> struct SlotPad {
+  static constexpr int value = 16;
+};
+template <class Op> struct SlotPad<Op, std::void_t<decltype(Op::SLOT_PAD)>> {
+  static constexpr int value = Op::SLOT_PAD;
+};
+template <class Op> using OpLayout = SiteLayout<typename Op::S, SlotPad<Op>::value>;
 
 // Per-site output block of a field op: OUT_ELEMS complex values (a
 // propagator-shaped 144 for diquark/sequential, 256 for the all-gamma meson).
@@ -107,7 +122,7 @@ template <class Op> struct OutLayout {
 //   tail            scalar ops: per-warp site values [CW][SPW][NOUT] (cx<R>)
 //                   field ops:  per-warp output staging [CW][2][SPW] slots
 template <class Op> struct Smem {
-  using L = SiteLayout<typename Op::S>;
+  using L = OpLayout<Op>;
   static constexpr size_t STAGE = (size_t)Op::NIN * Op::SITES * L::SLOT;
   static constexpr size_t STAGES = 128;
   static constexpr size_t EXTRA = STAGES + Op::NST * STAGE;
@@ -189,7 +204,7 @@ template <class Op>
 __device__ __forceinline__ void produce(const typename Op::Params &p, unsigned char *smem, uint64_t *full,
                                         uint64_t *empty, volatile int *abort_flag)
 {
-  using L = SiteLayout<typename Op::S>;
+  using L = OpLayout<Op>;
   constexpr int NST = Op::NST, NIN = Op::NIN, SITES = Op::SITES;
   const TileGeom &g = p.geom;
   const int lane = threadIdx.x & 31;
@@ -240,7 +255,7 @@ __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) scalar_kernel(c
 {
   using S = typename Op::S;
   using R = typename Op::R;
-  using L = SiteLayout<S>;
+  using L = OpLayout<Op>;
   constexpr int NIN = Op::NIN, SITES = Op::SITES, TPS = Op::TPS, NST = Op::NST, NOUT = Op::NOUT;
   constexpr int SPW = 32 / TPS, CW = Op::CW;
 
@@ -356,7 +371,7 @@ template <class Op>
 __global__ void __launch_bounds__(Op::THREADS, min_blocks<Op>()) field_kernel(const __grid_constant__ typename Op::Params p)
 {
   using S = typename Op::S;
-  using L = SiteLayout<S>;
+  using L = OpLayout<Op>;
   constexpr int NIN = Op::NIN, SITES = Op::SITES, TPS = Op::TPS, NST = Op::NST;
   constexpr int SPW = 32 / TPS, CW = Op::CW;
 

@@ -937,6 +937,11 @@ template <class R, class S, int CW, int NST, int NW, int MINB = 0>
 struct BaryonFusedSharedWedgeSameOp : OpBase<R, S, CW, 8, NST> {
   static constexpr int NIN = 2, NOUT = 6 * NW, EXTRA_BYTES = cbytes<S>(9 * NW + 8 * NW);
   static constexpr bool FIELD = false;
+  // Four sites share a warp here.  Their threads load colour blocks 4 i + x
+  // (x = 0..3, two rows i), 8-byte values at block * 72 bytes: with 1168-byte
+  // slots the next site's blocks land 16 bytes on, in banks the first site's
+  // blocks already use; 1184-byte slots move them 32 bytes on, clear of those.
+  static constexpr int SLOT_PAD = 32;
   static constexpr int MIN_CTAS = MINB;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
