@@ -9,23 +9,43 @@ __device__ DeviceStatus g_device_status;
 cudaError_t device_status_ptr(DeviceStatus **out) { return cudaGetSymbolAddress((void **)out, g_device_status); }
 
 // out.p[o][t] = sum_{parity, chunk} partial[((parity*lt + t)*chunks_per_seg + chunk)*nout + o]
-// Segments are half-timeslices in PyQUDA order [parity][t][...]; the sum runs
-// in FP64 in a fixed order, so results are bitwise reproducible.
-__global__ void finalize_kernel(const double2 *__restrict__ partial, OutPtrs out, int nout, int lt, int chunks_per_seg)
+// Segments are half-timeslices in PyQUDA order [parity][t][...].  One block of
+// kFinThreads threads per (o, t), block index o * lt + t: thread k sums the
+// partials k, k + kFinThreads, ... of the 2 * chunks_per_seg (parity-major) in
+// FP64, then a fixed shuffle tree and one shared-memory step join the threads.
+// The order is the same on every call, so results are bitwise reproducible.
+// (One thread per (o, t) walking every partial in turn left the sum's latency
+// chain on the critical path: 108 dependent loads per thread for a per-call
+// triangle at 24^3 x 64.)
+__global__ void __launch_bounds__(kFinThreads) finalize_kernel(const double2 *__restrict__ partial, OutPtrs out,
+                                                               int nout, int lt, int chunks_per_seg)
 {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nout * lt) return;
-  const int o = idx / lt, t = idx % lt;
+  const int o = blockIdx.x / lt, t = blockIdx.x - o * lt;
+  const int n = 2 * chunks_per_seg;
   double sx = 0.0, sy = 0.0;
-  for (int par = 0; par < 2; ++par) {
-    const double2 *row = partial + ((size_t)(par * lt + t) * chunks_per_seg) * nout + o;
-    for (int c = 0; c < chunks_per_seg; ++c) {
-      const double2 v = row[(size_t)c * nout];
-      sx += v.x;
-      sy += v.y;
-    }
+  for (int k = threadIdx.x; k < n; k += kFinThreads) {
+    const int par = k >= chunks_per_seg ? 1 : 0, c = k - par * chunks_per_seg;
+    const double2 v = partial[((size_t)(par * lt + t) * chunks_per_seg + c) * nout + o];
+    sx += v.x;
+    sy += v.y;
   }
-  out.p[o][t] = make_double2(sx, sy);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    sx += __shfl_down_sync(0xffffffffu, sx, off);
+    sy += __shfl_down_sync(0xffffffffu, sy, off);
+  }
+  __shared__ double2 wsum[kFinThreads / 32];
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = make_double2(sx, sy);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double2 r = wsum[0];
+#pragma unroll
+    for (int w = 1; w < kFinThreads / 32; ++w) {
+      r.x += wsum[w].x;
+      r.y += wsum[w].y;
+    }
+    out.p[o][t] = r;
+  }
 }
 
 // complex128 <-> complex64, one complex per thread step, grid-stride.

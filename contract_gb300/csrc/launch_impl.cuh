@@ -65,6 +65,7 @@ struct OutPtrs {
   double2 *p[16];
 };
 
+constexpr int kFinThreads = 64;  // finalize_kernel's block: the partials of one (output, timeslice)
 __global__ void finalize_kernel(const double2 *__restrict__ partial, OutPtrs out, int nout, int lt, int chunks_per_seg);
 
 template <class Op> cudaError_t run_scalar(const Job &job, OpParams<typename Op::R> p)
@@ -91,10 +92,9 @@ template <class Op> cudaError_t run_scalar(const Job &job, OpParams<typename Op:
   scalar_kernel<Op><<<grid, Op::THREADS, smem, job.stream>>>(p);
   e = cudaGetLastError();
   if (e != cudaSuccess || job.per_site) return e;
-  const int n = Op::NOUT * job.lt;
   // partial is [segment][chunk][consumer warp][NOUT]: fold the warps into the chunk count.
-  finalize_kernel<<<(n + 127) / 128, 128, 0, job.stream>>>(partial, user_out, Op::NOUT, job.lt,
-                                                            p.geom.chunks_per_seg * Op::CW);
+  finalize_kernel<<<Op::NOUT * job.lt, kFinThreads, 0, job.stream>>>(partial, user_out, Op::NOUT, job.lt,
+                                                                      p.geom.chunks_per_seg * Op::CW);
   return cudaGetLastError();
 }
 
