@@ -37,7 +37,7 @@ static cudaError_t run_batch(const Job &job, const OpParams<typename Op::R> &op,
     ji.half_slice = (long long)specs[i].latt[0] * specs[i].latt[1] * specs[i].latt[2] / 2;
     BatchItem &it = bp.items[i];
     for (int q = 0; q < 3; ++q) it.in[q] = specs[i].in[q];
-    it.geom = make_geom(ji, Op::SITES, job.num_sms);
+    it.geom = make_geom(ji, Op::SITES, job.num_sms, 8);  // the device queue balances the CTAs
     it.chunk_begin = chunks;
     it.lt = ji.lt;
     it.out = specs[i].out;
