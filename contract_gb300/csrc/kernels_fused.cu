@@ -7,6 +7,14 @@ namespace cgb {
 // Projectors spanned by at most `nw` gamma matrices (e.g. (1 +- g4)/2): no N' buffers.
 using FusedCliff1P = BaryonFusedCliffOp<double, double2, 4, 16, 2, 1>;
 using FusedCliff2P = BaryonFusedCliffOp<double, double2, 4, 16, 2, 2>;
+// complex128 runs on the FP64 pipe, so its time follows the FP64 FMA count: the
+// shared-wedge forms do a third fewer (5 078 complex FMA per site with two
+// two-term projectors against 7 382), and with one field for P_i and P_j the
+// one-pass form about half.
+using SharedWedge1P = BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 1>;
+using SharedWedge2P = BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 2>;
+using SharedSame1P = BaryonFusedSharedWedgeSameOp<double, double2, 4, 2, 1>;
+using SharedSame2P = BaryonFusedSharedWedgeSameOp<double, double2, 4, 2, 2>;
 // General projectors: N'_w = W_w N materialised per site.
 using Fused1P = BaryonFusedOp<double, double2, 4, 16, 2, 1>;
 using Fused2P = BaryonFusedOp<double, double2, 4, 16, 2, 2>;
@@ -56,10 +64,12 @@ static const VariantSet<float, 12> kFusedCliff2M = {
 // shared-wedge form also forms each distinct wedge once (eight threads per
 // site); it needs a Gamma_ij permutation without fixed points and takes the
 // one-pass merged form otherwise.
-template <class Op> cudaError_t run_same_field(const Job &job, OpParams<float> q)
+template <class Op> cudaError_t run_same_field(const Job &job, OpParams<typename Op::R> q)
 {
+  using R = typename Op::R;
   if (q.b.perm1[0] == 0) {  // XOR permutations: a fixed point at 0 means the identity
-    using Fallback = BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, Op::NOUT / 6, 3, true>;
+    constexpr int kMinb = sizeof(R) == 4 ? 3 : 0;
+    using Fallback = BaryonFusedCliffMergedOp<R, typename Op::S, 4, 16, 2, Op::NOUT / 6, kMinb, true>;
     return run_scalar<Fallback>(job, q);
   }
   q.in[1] = q.in[2];  // inputs: the field once, then P_n
@@ -92,7 +102,7 @@ static const VariantSet<float, 7> kFusedCliff2MSame = {
 // The shared-wedge forms derive the Gamma_kl^T variant of each type from the
 // Gamma_kl one by the phase ph2[1] - ph2[0], which is the same in every column
 // because every Gamma(n) is symmetric or antisymmetric; checked here all the same.
-static bool kl_transpose_is_sign(const OpParams<float> &q)
+template <class R> static bool kl_transpose_is_sign(const OpParams<R> &q)
 {
   const int d = (q.b.ph2[1][0] - q.b.ph2[0][0]) & 3;
   for (int c = 1; c < 4; ++c)
@@ -104,6 +114,11 @@ cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &
 {
   const bool cliff = p.b.cl.ng <= nw;
   if (job.prec == Prec::C128) {
+    if (cliff && kl_transpose_is_sign(p)) {
+      if (fused_same_ij(p))
+        return nw == 1 ? run_same_field<SharedSame1P>(job, p) : run_same_field<SharedSame2P>(job, p);
+      return nw == 1 ? run_scalar<SharedWedge1P>(job, p) : run_scalar<SharedWedge2P>(job, p);
+    }
     if (cliff) return nw == 1 ? run_scalar<FusedCliff1P>(job, p) : run_scalar<FusedCliff2P>(job, p);
     return nw == 1 ? run_scalar<Fused1P>(job, p) : run_scalar<Fused2P>(job, p);
   }

@@ -185,6 +185,24 @@ def test_fused_all_types_one_and_four_term_projectors(api, props, c_oracle):
             assert per_t_rel(got64[t, 0], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
 
 
+def test_fused_same_field_c128(api, props, c_oracle):
+    """complex128 with one pointer for P_i and P_j: the one-pass shared-wedge form
+    (and, for Gamma_ij = g5, whose permutation has fixed points, the merged
+    one-pass form), one and two projectors, against the oracle."""
+    pi, _, pn = props
+    pp = api.projector_plus_minus()
+    a, c = cuda(pi), cuda(pn)
+    for gij, gkl in ((5, 5), (15, 5)):
+        ref = np.zeros((6, 2, LATT[3]), np.complex128)
+        for t in range(6):
+            for w in range(2):
+                ref[t, w] = eo.timeslice_sum(c_oracle.baryon_general_two_point(pi, pi, pn, t, gij, gkl, pp[w]), LATT)
+        got = api.baryon_all_types(a, a, c, gij, gkl, pp, latt=LATT).cpu().numpy()
+        assert rel_err(got, ref) < TOL_C128, (gij, gkl)
+        got1 = api.baryon_all_types(a, a, c, gij, gkl, pp[:1], latt=LATT).cpu().numpy()
+        assert rel_err(got1[:, 0], ref[:, 0]) < TOL_C128, (gij, gkl)
+
+
 def test_fused_same_field_for_i_and_j(api, props, c_oracle):
     """P_i and P_j passed as one pointer (the u quark of a proton): the complex64
     fused pass evaluates one triangle pass instead of two; per call, in a batch
