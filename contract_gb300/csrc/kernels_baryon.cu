@@ -4,10 +4,24 @@
 
 namespace cgb {
 
-// complex128 (FP64-pipe bound): 8 sites per tile, one (i, l) spin pair per thread.
-using LoopP = BaryonLoopOp<double, double2, 4, 16, 3>;
-using TriP = BaryonTriOp<double, double2, 4, 16, 3>;
-using TriCliffP = BaryonTriCliffOp<double, double2, 4, 16, 3>;
+// complex128 (FP64-pipe bound), one (i, l) spin pair per thread: four consumer
+// warps and three ring stages (one CTA per SM: 8 sites x 3 inputs x 2 320 B per
+// stage), or smaller tiles and rings so that two or three CTAs fit.
+static const VariantSet<double, 4> kLoopP = {
+  {run_scalar<BaryonLoopOp<double, double2, 4, 16, 3>>, run_scalar<BaryonLoopOp<double, double2, 3, 16, 2>>,
+   run_scalar<BaryonLoopOp<double, double2, 2, 16, 3>>, run_scalar<BaryonLoopOp<double, double2, 2, 16, 2>>},
+  {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3", "cw2.tps16.st2"},
+  0};
+static const VariantSet<double, 4> kTriP = {
+  {run_scalar<BaryonTriOp<double, double2, 4, 16, 3>>, run_scalar<BaryonTriOp<double, double2, 3, 16, 2>>,
+   run_scalar<BaryonTriOp<double, double2, 2, 16, 3>>, run_scalar<BaryonTriOp<double, double2, 2, 16, 2>>},
+  {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3", "cw2.tps16.st2"},
+  0};
+static const VariantSet<double, 4> kTriCliffP = {
+  {run_scalar<BaryonTriCliffOp<double, double2, 4, 16, 3>>, run_scalar<BaryonTriCliffOp<double, double2, 3, 16, 2>>,
+   run_scalar<BaryonTriCliffOp<double, double2, 2, 16, 3>>, run_scalar<BaryonTriCliffOp<double, double2, 2, 16, 2>>},
+  {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3", "cw2.tps16.st2"},
+  0};
 
 // complex64 variants: sites per tile x ring depth x CTAs per SM.
 static const VariantSet<float, 4> kLoopM = {
@@ -33,8 +47,8 @@ cudaError_t launch_baryon(const Job &job, bool loop, const OpParams<double> &p)
   // A projector that is one gamma matrix (baryon_two_point) needs no N' buffer.
   const bool cliff = p.b.cl.ng == 1;
   if (job.prec == Prec::C128) {
-    if (loop) return run_scalar<LoopP>(job, p);
-    return cliff ? run_scalar<TriCliffP>(job, p) : run_scalar<TriP>(job, p);
+    if (loop) return kLoopP.launch(job, p);
+    return cliff ? kTriCliffP.launch(job, p) : kTriP.launch(job, p);
   }
   const OpParams<float> q = convert_params<float>(p);
   if (loop) return kLoopM.launch(job, q);
@@ -43,7 +57,10 @@ cudaError_t launch_baryon(const Job &job, bool loop, const OpParams<double> &p)
 
 int baryon_variants(Prec prec, int form, const char *const **names)
 {
-  if (prec == Prec::C128) return 1;
+  if (prec == Prec::C128) {
+    if (form == 0) return kLoopP.describe(names);
+    return form == 1 ? kTriCliffP.describe(names) : kTriP.describe(names);
+  }
   if (form == 0) return kLoopM.describe(names);
   return form == 1 ? kTriCliffM.describe(names) : kTriM.describe(names);
 }

@@ -1,9 +1,10 @@
 """Child process of test_parity_gpu.test_baryon_variants_forced: runs the
-per-call complex64 baryon two-point (loop and triangle forms) on small
+per-call baryon two-point (loop and triangle forms, complex64 or complex128) on small
 lattices whose tune-cache entries (written by the parent into
 CONTRACT_TUNE_CACHE) force one tile-shape variant each, and prints, as one
-JSON line, each run's per-timeslice error against the FP64 oracle relative to
-max(|C_t|, sigma_t), with the tuner's report."""
+JSON line, each run's per-timeslice error against the FP64 oracle (complex64:
+relative to max(|C_t|, sigma_t); complex128: to the largest |C_t|), with the
+tuner's report."""
 import ctypes
 import json
 import os
@@ -24,21 +25,23 @@ def main():
     from contract_gb300 import _lib, api
     lib = _lib.lib()
     lib.contract_set_error_mode(1)
-    cases = json.loads(sys.argv[1])  # [[latt, contract_type, projector: "g4", "pp" or "dense"], ...]
+    # [[latt, contract_type, projector: "g4", "pp" or "dense", precision: 1 complex64, 0 complex128], ...]
+    cases = json.loads(sys.argv[1])
     oracle = L.c_oracle()
     rng = np.random.default_rng(17)
     projs = {"pp": np.ascontiguousarray(api.projector_plus_minus()[0]),  # (1 + g4)/2: two gamma-basis terms
              "dense": np.ascontiguousarray((rng.standard_normal(16) + 1j * rng.standard_normal(16)) / 4)}
     errs = []
-    for k, (latt, ctype, kind) in enumerate(cases):
+    for k, (latt, ctype, kind, prec) in enumerate(cases):
         use_proj = kind != "g4"
         proj = projs.get(kind)
         latt = tuple(latt)
         props = [eo.make_propagator(latt, 300 + 3 * k + s, 0.2 + 0.05 * s) for s in range(3)]
-        dev = [torch.from_numpy(p).cuda().to(torch.complex64) for p in props]
+        dtype = torch.complex64 if prec == 1 else torch.complex128
+        dev = [torch.from_numpy(p).cuda().to(dtype) for p in props]
         out = torch.full((latt[3],), float("nan"), dtype=torch.complex128, device="cuda")
         lib.contract_baryon(out.data_ptr(), *(d.data_ptr() for d in dev), ctype, props[0].shape[0], 5, 5, 8,
-                            proj.ctypes.data if use_proj else None, 1, (ctypes.c_int * 4)(*latt))
+                            proj.ctypes.data if use_proj else None, prec, (ctypes.c_int * 4)(*latt))
         got = out.cpu().numpy()
         if lib.contract_last_error():
             raise RuntimeError(lib.contract_last_error_message().decode())
@@ -46,7 +49,10 @@ def main():
                 else oracle.baryon_two_point(*props, ctype, 5, 5, 8))
         ref = eo.timeslice_sum(site, latt)
         sig = np.sqrt(eo.timeslice_sum(np.abs(site) ** 2, latt).real)
-        errs.append(float((np.abs(got - ref) / np.maximum(np.abs(ref), sig)).max()))
+        if prec == 1:  # relative to max(|C_t|, sigma_t)
+            errs.append(float((np.abs(got - ref) / np.maximum(np.abs(ref), sig)).max()))
+        else:  # complex128: relative to the largest |C_t|
+            errs.append(float(np.abs(got - ref).max() / np.abs(ref).max()))
     buf = ctypes.create_string_buffer(16384)
     lib.contract_autotune_report(buf, len(buf))
     print(json.dumps({"errors": errs, "report": buf.value.decode()}))
