@@ -30,15 +30,26 @@ static const VariantSet<float, 6> kDiquarkM = {
    "cw3.tps16.st3.direct"},
   0};
 
+// complex128 (FP64-pipe bound): the first shape is the default.
+static const VariantSet<double, 3> kDiquarkP = {
+  {run_field<DiquarkOp<double, double2, 4, 16, 3>>, run_field<DiquarkOp<double, double2, 3, 16, 2>>,
+   run_field<DiquarkOp<double, double2, 2, 16, 3>>},
+  {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3"},
+  0};
+
 cudaError_t launch_diquark(const Job &job, const OpParams<double> &p)
 {
-  if (job.prec == Prec::C128) return run_field<DiquarkOp<double, double2, 4, 16, 3>>(job, p);
+  if (job.prec == Prec::C128) return kDiquarkP.launch(job, p);
   return kDiquarkM.launch(job, convert_params<float>(p));
 }
 
 cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParams<double> &p)
 {
-  if (job.prec == Prec::C128) return seq_dispatch<double, double2, 4, 16, 3>(job, loop, role, p);
+  if (job.prec == Prec::C128) {
+    if (job.variant == 1) return seq_dispatch<double, double2, 3, 16, 2>(job, loop, role, p);
+    if (job.variant == 2) return seq_dispatch<double, double2, 2, 16, 3>(job, loop, role, p);
+    return seq_dispatch<double, double2, 4, 16, 3>(job, loop, role, p);
+  }
   const OpParams<float> q = convert_params<float>(p);
   if (job.variant == 1) return seq_dispatch<float, float2, 8, 16, 3>(job, loop, role, q);
   if (job.variant == 2) return seq_dispatch<float, float2, 3, 16, 3>(job, loop, role, q);
@@ -46,10 +57,15 @@ cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParam
 }
 
 static const char *const kSequentialNames[3] = {"cw5.tps16.st2", "cw8.tps16.st3", "cw3.tps16.st3"};
+static const char *const kSequentialNamesP[3] = {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3"};
 
 int field_variants(Prec prec, bool sequential, const char *const **names)
 {
-  if (prec == Prec::C128) return 1;
+  if (prec == Prec::C128) {
+    if (!sequential) return kDiquarkP.describe(names);
+    if (names) *names = kSequentialNamesP;
+    return 3;
+  }
   if (!sequential) return kDiquarkM.describe(names);
   if (names) *names = kSequentialNames;
   return 3;

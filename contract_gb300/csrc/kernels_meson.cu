@@ -4,10 +4,23 @@
 
 namespace cgb {
 
-// complex128: FP64-pipe bound; 8 sites per tile, two CTAs per SM.
-using MesonP = MesonOp<double, double2, 2, 8, 3>;
-using MesonAllSrcP = MesonAllSourceOp<double, double2, 1, 3>;
-using MesonAllSnkP = MesonAllSinkOp<double, double2, 1, 3>;
+// complex128: FP64-pipe bound.  The first shape of each set is the default;
+// the others trade ring depth against CTAs per SM.
+static const VariantSet<double, 4> kMesonP = {
+  {run_scalar<MesonOp<double, double2, 2, 8, 3>>, run_scalar<MesonOp<double, double2, 4, 8, 2>>,
+   run_scalar<MesonOp<double, double2, 2, 8, 2>>, run_scalar<MesonOp<double, double2, 3, 8, 3>>},
+  {"cw2.tps8.st3", "cw4.tps8.st2", "cw2.tps8.st2", "cw3.tps8.st3"},
+  0};
+static const VariantSet<double, 3> kMesonAllSrcP = {
+  {run_scalar<MesonAllSourceOp<double, double2, 1, 3>>, run_scalar<MesonAllSourceOp<double, double2, 2, 2>>,
+   run_scalar<MesonAllSourceOp<double, double2, 1, 2>>},
+  {"cw1.tps4.st3", "cw2.tps4.st2", "cw1.tps4.st2"},
+  0};
+static const VariantSet<double, 3> kMesonAllSnkP = {
+  {run_scalar<MesonAllSinkOp<double, double2, 1, 3>>, run_scalar<MesonAllSinkOp<double, double2, 2, 2>>,
+   run_scalar<MesonAllSinkOp<double, double2, 1, 2>>},
+  {"cw1.tps4.st3", "cw2.tps4.st2", "cw1.tps4.st2"},
+  0};
 
 // complex64: HBM bound; the variants trade ring depth against CTAs per SM.
 static const VariantSet<float, 4> kMesonM = {
@@ -18,7 +31,7 @@ static const VariantSet<float, 4> kMesonM = {
 
 cudaError_t launch_meson(const Job &job, const OpParams<double> &p)
 {
-  if (job.prec == Prec::C128) return run_scalar<MesonP>(job, p);
+  if (job.prec == Prec::C128) return kMesonP.launch(job, p);
   return kMesonM.launch(job, convert_params<float>(p));
 }
 
@@ -38,21 +51,20 @@ static const VariantSet<float, 4> kMesonAllSnkM = {
 
 cudaError_t launch_meson_all(const Job &job, bool source, const OpParams<double> &p)
 {
-  if (job.prec == Prec::C128)
-    return source ? run_scalar<MesonAllSrcP>(job, p) : run_scalar<MesonAllSnkP>(job, p);
+  if (job.prec == Prec::C128) return source ? kMesonAllSrcP.launch(job, p) : kMesonAllSnkP.launch(job, p);
   const OpParams<float> q = convert_params<float>(p);
   return source ? kMesonAllSrcM.launch(job, q) : kMesonAllSnkM.launch(job, q);
 }
 
 int meson_all_variants(Prec prec, bool source, const char *const **names)
 {
-  if (prec == Prec::C128) return 1;
+  if (prec == Prec::C128) return source ? kMesonAllSrcP.describe(names) : kMesonAllSnkP.describe(names);
   return source ? kMesonAllSrcM.describe(names) : kMesonAllSnkM.describe(names);
 }
 
 int meson_variants(Prec prec, const char *const **names)
 {
-  if (prec == Prec::C128) return 1;
+  if (prec == Prec::C128) return kMesonP.describe(names);
   return kMesonM.describe(names);
 }
 

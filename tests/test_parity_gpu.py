@@ -547,6 +547,53 @@ def test_baryon_variants_forced(tmp_path):
         assert err < (TOL_C64_TIMESLICE if case[3] == 1 else TOL_C128), (name, case, err)
 
 
+def test_site_variants_forced(tmp_path):
+    """Every compiled tile-shape variant of the meson (one Gamma pair,
+    all-source, all-sink), diquark and sequential-source kernels, in complex64
+    and complex128, forced through a tune cache, against the FP64 oracle.
+    Each case uses its own lattice shape, so that each tune key fixes one
+    variant."""
+    import ctypes
+    import json
+    import os
+    import subprocess
+    import sys
+    from contract_gb300 import _lib, build
+    build.build()
+    lib = _lib.lib()
+    cache = tmp_path / "tune.txt"
+    lines, cases, names = [], [], []
+    # (op, tune kind, aux, contract type, sequential slot); sequential aux = 3 (loop types) + slot
+    ops = (("meson", 0, 0, 0, 0), ("meson_all_source", 6, 1, 0, 0), ("meson_all_sink", 6, 0, 0, 0),
+           ("diquark", 4, 0, 0, 0), ("sequential", 5, 5, 0, 2), ("sequential", 5, 0, 1, 0))
+    for prec in (1, 0):
+        for c, (op, kind, aux, ctype, slot) in enumerate(ops):
+            buf = ctypes.create_string_buffer(4096)
+            n = lib.contract_variant_names(kind, prec, aux, buf, len(buf))
+            vnames = buf.value.decode().split()
+            assert n == len(vnames) >= 3, (op, prec, vnames)
+            per_site = op in ("diquark", "sequential")
+            for v, name in enumerate(vnames):
+                latt = (4, 2, 2 + 2 * c, 3 + v)  # one lattice shape per (case, variant); the key holds prec
+                vol = int(np.prod(latt))
+                lt, half = (0, 0) if per_site else (latt[3], vol // latt[3] // 2)
+                lines.append(f"kind={kind},prec={prec},aux={aux},volume={vol},lt={lt},half={half}\t{v} {name} 1.0\n")
+                cases.append([op, list(latt), prec, ctype, slot])
+                names.append(name)
+    cache.write_text("".join(lines))
+    env = dict(os.environ, CONTRACT_TUNE_CACHE=str(cache), CONTRACT_AUTOTUNE="0")
+    child = os.path.join(os.path.dirname(os.path.abspath(__file__)), "site_variants_child.py")
+    res = subprocess.run([sys.executable, child, json.dumps(cases)], env=env, capture_output=True, text=True,
+                         timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    out = json.loads(res.stdout.strip().splitlines()[-1])
+    for name in set(names):
+        assert name in out["report"], (name, out["report"])
+    # complex64: the inputs rounded to complex64 against FP64 ones, relative to the largest value
+    for name, case, err in zip(names, cases, out["errors"]):
+        assert err < (2e-6 if case[2] == 1 else TOL_C128), (name, case, err)
+
+
 def test_momentum_variants_forced(tmp_path):
     """Each tile-shape variant of the momentum projection, forced through a tune
     cache: tensor-core work units of 192 k-steps (six units per timeslice on
