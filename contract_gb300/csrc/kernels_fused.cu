@@ -11,8 +11,19 @@ using FusedCliff2P = BaryonFusedCliffOp<double, double2, 4, 16, 2, 2>;
 // shared-wedge forms do a third fewer (5 078 complex FMA per site with two
 // two-term projectors against 7 382), and with one field for P_i and P_j the
 // one-pass form about half.
-using SharedWedge1P = BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 1>;
-using SharedWedge2P = BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 2>;
+// The first shape is the default; the smaller tiles let two CTAs share an SM.
+static const VariantSet<double, 3> kSharedWedge1P = {
+  {run_scalar<BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 1>>,
+   run_scalar<BaryonFusedSharedWedgeOp<double, double2, 3, 16, 2, 1>>,
+   run_scalar<BaryonFusedSharedWedgeOp<double, double2, 2, 16, 3, 1>>},
+  {"shared.cw4.tps16.st2", "shared.cw3.tps16.st2", "shared.cw2.tps16.st3"},
+  0};
+static const VariantSet<double, 3> kSharedWedge2P = {
+  {run_scalar<BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 2>>,
+   run_scalar<BaryonFusedSharedWedgeOp<double, double2, 3, 16, 2, 2>>,
+   run_scalar<BaryonFusedSharedWedgeOp<double, double2, 2, 16, 3, 2>>},
+  {"shared.cw4.tps16.st2", "shared.cw3.tps16.st2", "shared.cw2.tps16.st3"},
+  0};
 using SharedSame1P = BaryonFusedSharedWedgeSameOp<double, double2, 4, 2, 1>;
 using SharedSame2P = BaryonFusedSharedWedgeSameOp<double, double2, 4, 2, 2>;
 // General projectors: N'_w = W_w N materialised per site.
@@ -117,7 +128,7 @@ cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &
     if (cliff && kl_transpose_is_sign(p)) {
       if (fused_same_ij(p))
         return nw == 1 ? run_same_field<SharedSame1P>(job, p) : run_same_field<SharedSame2P>(job, p);
-      return nw == 1 ? run_scalar<SharedWedge1P>(job, p) : run_scalar<SharedWedge2P>(job, p);
+      return nw == 1 ? kSharedWedge1P.launch(job, p) : kSharedWedge2P.launch(job, p);
     }
     if (cliff) return nw == 1 ? run_scalar<FusedCliff1P>(job, p) : run_scalar<FusedCliff2P>(job, p);
     return nw == 1 ? run_scalar<Fused1P>(job, p) : run_scalar<Fused2P>(job, p);
@@ -138,8 +149,10 @@ cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &
 // aux = nw + 4 * (P_i and P_j one field)
 int fused_variants(Prec prec, int aux, const char *const **names)
 {
-  if (prec == Prec::C128) return 1;
   const int nw = aux & 3;
+  // complex128: the shapes of the two-field shared-wedge form (the form the
+  // launcher picks for gamma-basis projectors; the others run one shape)
+  if (prec == Prec::C128) return (aux & 4) ? 1 : (nw == 1 ? kSharedWedge1P.describe(names) : kSharedWedge2P.describe(names));
   if (aux & 4) return nw == 1 ? kFusedCliff1MSame.describe(names) : kFusedCliff2MSame.describe(names);
   return nw == 1 ? kFusedCliff1M.describe(names) : kFusedCliff2M.describe(names);
 }

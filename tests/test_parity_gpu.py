@@ -462,10 +462,10 @@ def test_meson_momentum_many_z_groups(api):
 
 
 def test_fused_variants_forced(tmp_path):
-    """Every compiled tile-shape variant of the complex64 fused all-types pass
-    (shared-wedge, merged and two-loop forms; two and one projector; two
-    fields and one field for P_i and P_j), forced through a tune cache, against
-    the FP64 oracle.  Each case uses its own lattice shape, so that each tune
+    """Every compiled tile-shape variant of the fused all-types pass (complex64:
+    shared-wedge, merged and two-loop forms, two and one projector, two fields
+    and one field for P_i and P_j; complex128: the shared-wedge shapes), forced
+    through a tune cache, against the FP64 oracle.  Each case uses its own lattice shape, so that each tune
     key fixes one variant."""
     import ctypes
     import json
@@ -477,18 +477,19 @@ def test_fused_variants_forced(tmp_path):
     lib = _lib.lib()
     cache = tmp_path / "tune.txt"
     lines, cases, names = [], [], []
-    for nproj, same in ((2, False), (1, False), (2, True), (1, True)):
+    for prec, nproj, same in ((1, 2, False), (1, 1, False), (1, 2, True), (1, 1, True), (0, 2, False),
+                              (0, 1, False)):
         aux = nproj + (4 if same else 0)
         buf = ctypes.create_string_buffer(4096)
-        n = lib.contract_variant_names(3, 1, aux, buf, len(buf))  # op 3: the fused all-types pass
+        n = lib.contract_variant_names(3, prec, aux, buf, len(buf))  # op 3: the fused all-types pass
         vnames = buf.value.decode().split()
-        assert n == len(vnames) >= 7, (n, vnames)
+        assert n == len(vnames) >= (7 if prec == 1 else 3), (n, vnames)
         for v, name in enumerate(vnames):
             latt = (4, 2, 2 + 2 * same, 2 + v) if nproj == 2 else (2, 4, 2 + 2 * same, 2 + v)
             vol = int(np.prod(latt))
-            key = f"kind=3,prec=1,aux={aux},volume={vol},lt={latt[3]},half={vol // latt[3] // 2}"
+            key = f"kind=3,prec={prec},aux={aux},volume={vol},lt={latt[3]},half={vol // latt[3] // 2}"
             lines.append(f"{key}\t{v} {name} 1.0\n")
-            cases.append([list(latt), nproj, same])
+            cases.append([list(latt), nproj, same, prec])
             names.append(name)
     cache.write_text("".join(lines))
     env = dict(os.environ, CONTRACT_TUNE_CACHE=str(cache), CONTRACT_AUTOTUNE="0")
@@ -500,7 +501,7 @@ def test_fused_variants_forced(tmp_path):
     for name in set(names):
         assert name in out["report"], (name, out["report"])
     for name, case, err in zip(names, cases, out["errors"]):
-        assert err < TOL_C64_TIMESLICE, (name, case, err)
+        assert err < (TOL_C64_TIMESLICE if case[3] == 1 else TOL_C128), (name, case, err)
 
 
 def test_baryon_variants_forced(tmp_path):
