@@ -272,8 +272,7 @@ __global__ void __launch_bounds__(FusedShape<SW>::THREADS, 1)
       else if constexpr (SAME) site_products_same_half(in[0], sub, dst);
       else if constexpr (SW == 8) site_products(in[0], in[1], sub, dst);
       else site_products_half(in[0], in[1], sub, dst);
-      __threadfence_block();
-      __syncwarp();
+      __syncwarp();  // the lanes' product stores, then lane 0's arrive (release) publishes them
       if (lane == 0) mbar_arrive(&ofull[ob]);
     }
     return;
@@ -501,8 +500,7 @@ __global__ void __launch_bounds__(FusedShape<SW>::THREADS, 1)
       else if constexpr (SAME) site_products_same_half(in[0], sub, dst);
       else if constexpr (SW == 8) site_products(in[0], in[1], sub, dst);
       else site_products_half(in[0], in[1], sub, dst);
-      __threadfence_block();
-      __syncwarp();
+      __syncwarp();  // the lanes' product stores, then lane 0's arrive (release) publishes them
       if (lane == 0) mbar_arrive(&ofull[ob]);
     }
     return;
