@@ -6,41 +6,44 @@ namespace cgb {
 
 // complex128 (FP64-pipe bound), one (i, l) spin pair per thread: four consumer
 // warps and three ring stages (one CTA per SM: 8 sites x 3 inputs x 2 320 B per
-// stage), or smaller tiles and rings so that two or three CTAs fit.
+// stage), or smaller tiles and rings so that two or three CTAs fit.  The
+// default (used with autotuning off) is three consumer warps and two stages,
+// the tuner's choice at 24^3 x 64.
 static const VariantSet<double, 4> kLoopP = {
   {run_scalar<BaryonLoopOp<double, double2, 4, 16, 3>>, run_scalar<BaryonLoopOp<double, double2, 3, 16, 2>>,
    run_scalar<BaryonLoopOp<double, double2, 2, 16, 3>>, run_scalar<BaryonLoopOp<double, double2, 2, 16, 2>>},
   {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3", "cw2.tps16.st2"},
-  0};
+  1};
 static const VariantSet<double, 4> kTriP = {
   {run_scalar<BaryonTriOp<double, double2, 4, 16, 3>>, run_scalar<BaryonTriOp<double, double2, 3, 16, 2>>,
    run_scalar<BaryonTriOp<double, double2, 2, 16, 3>>, run_scalar<BaryonTriOp<double, double2, 2, 16, 2>>},
   {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3", "cw2.tps16.st2"},
-  0};
+  1};
 static const VariantSet<double, 4> kTriCliffP = {
   {run_scalar<BaryonTriCliffOp<double, double2, 4, 16, 3>>, run_scalar<BaryonTriCliffOp<double, double2, 3, 16, 2>>,
    run_scalar<BaryonTriCliffOp<double, double2, 2, 16, 3>>, run_scalar<BaryonTriCliffOp<double, double2, 2, 16, 2>>},
   {"cw4.tps16.st3", "cw3.tps16.st2", "cw2.tps16.st3", "cw2.tps16.st2"},
-  0};
+  1};
 
-// complex64 variants: sites per tile x ring depth x CTAs per SM.
+// complex64 variants: sites per tile x ring depth x CTAs per SM; the default
+// (last field) is the tuner's choice at 24^3 x 64.
 static const VariantSet<float, 4> kLoopM = {
   {run_scalar<BaryonLoopOp<float, float2, 7, 16, 2>>, run_scalar<BaryonLoopOp<float, float2, 5, 16, 3>>,
    run_scalar<BaryonLoopOp<float, float2, 4, 8, 3>>, run_scalar<BaryonLoopOp<float, float2, 3, 16, 3>>},
   {"cw7.tps16.st2", "cw5.tps16.st3", "cw4.tps8.st3", "cw3.tps16.st3"},
-  0};
+  3};
 // General projector (N' materialised per site).
 static const VariantSet<float, 4> kTriM = {
   {run_scalar<BaryonTriOp<float, float2, 6, 16, 2>>, run_scalar<BaryonTriOp<float, float2, 7, 16, 3>>,
    run_scalar<BaryonTriOp<float, float2, 4, 16, 3>>, run_scalar<BaryonTriOp<float, float2, 3, 16, 2>>},
   {"cw6.tps16.st2", "cw7.tps16.st3", "cw4.tps16.st3", "cw3.tps16.st2"},
-  0};
+  3};
 static const VariantSet<float, 5> kTriCliffM = {
   {run_scalar<BaryonTriCliffOp<float, float2, 7, 16, 2>>, run_scalar<BaryonTriCliffOp<float, float2, 5, 16, 3>>,
    run_scalar<BaryonTriCliffOp<float, float2, 4, 8, 2>>, run_scalar<BaryonTriCliffOp<float, float2, 3, 16, 2>>,
    run_scalar<BaryonTriCliffOp<float, float2, 4, 16, 3>>},
   {"cw7.tps16.st2", "cw5.tps16.st3", "cw4.tps8.st2", "cw3.tps16.st2", "cw4.tps16.st3"},
-  0};
+  3};
 
 cudaError_t launch_baryon(const Job &job, bool loop, const OpParams<double> &p)
 {

@@ -21,14 +21,15 @@ static cudaError_t seq_dispatch(const Job &job, bool loop, int role, const OpPar
   }
 }
 
-// complex64 variants: the two-CTA shapes keep more tiles (and stores) in flight.
+// complex64 variants: the two-CTA shapes keep more tiles (and stores) in flight;
+// the default (last field) is the tuner's choice at 24^3 x 64.
 static const VariantSet<float, 6> kDiquarkM = {
   {run_field<DiquarkOp<float, float2, 6, 16, 2>>, run_field<DiquarkOp<float, float2, 8, 16, 3>>,
    run_field<DiquarkOp<float, float2, 6, 16, 2, true>>, run_field<DiquarkOp<float, float2, 8, 16, 3, true>>,
    run_field<DiquarkOp<float, float2, 4, 16, 2, true>>, run_field<DiquarkOp<float, float2, 3, 16, 3, true>>},
   {"cw6.tps16.st2", "cw8.tps16.st3", "cw6.tps16.st2.direct", "cw8.tps16.st3.direct", "cw4.tps16.st2.direct",
    "cw3.tps16.st3.direct"},
-  0};
+  5};
 
 // complex128 (FP64-pipe bound): the first shape is the default.
 static const VariantSet<double, 3> kDiquarkP = {
@@ -45,10 +46,10 @@ cudaError_t launch_diquark(const Job &job, const OpParams<double> &p)
 
 cudaError_t launch_sequential(const Job &job, bool loop, int role, const OpParams<double> &p)
 {
-  if (job.prec == Prec::C128) {
-    if (job.variant == 1) return seq_dispatch<double, double2, 3, 16, 2>(job, loop, role, p);
+  if (job.prec == Prec::C128) {  // default (no variant chosen): three consumer warps, two stages
+    if (job.variant == 0) return seq_dispatch<double, double2, 4, 16, 3>(job, loop, role, p);
     if (job.variant == 2) return seq_dispatch<double, double2, 2, 16, 3>(job, loop, role, p);
-    return seq_dispatch<double, double2, 4, 16, 3>(job, loop, role, p);
+    return seq_dispatch<double, double2, 3, 16, 2>(job, loop, role, p);
   }
   const OpParams<float> q = convert_params<float>(p);
   if (job.variant == 1) return seq_dispatch<float, float2, 8, 16, 3>(job, loop, role, q);

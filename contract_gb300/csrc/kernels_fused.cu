@@ -11,19 +11,20 @@ using FusedCliff2P = BaryonFusedCliffOp<double, double2, 4, 16, 2, 2>;
 // shared-wedge forms do a third fewer (5 078 complex FMA per site with two
 // two-term projectors against 7 382), and with one field for P_i and P_j the
 // one-pass form about half.
-// The first shape is the default; the smaller tiles let two CTAs share an SM.
+// The smaller tiles let two CTAs share an SM; the default (last field) is the
+// six-site tile, the tuner's choice at 24^3 x 64.
 static const VariantSet<double, 3> kSharedWedge1P = {
   {run_scalar<BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 1>>,
    run_scalar<BaryonFusedSharedWedgeOp<double, double2, 3, 16, 2, 1>>,
    run_scalar<BaryonFusedSharedWedgeOp<double, double2, 2, 16, 3, 1>>},
   {"shared.cw4.tps16.st2", "shared.cw3.tps16.st2", "shared.cw2.tps16.st3"},
-  0};
+  1};
 static const VariantSet<double, 3> kSharedWedge2P = {
   {run_scalar<BaryonFusedSharedWedgeOp<double, double2, 4, 16, 2, 2>>,
    run_scalar<BaryonFusedSharedWedgeOp<double, double2, 3, 16, 2, 2>>,
    run_scalar<BaryonFusedSharedWedgeOp<double, double2, 2, 16, 3, 2>>},
   {"shared.cw4.tps16.st2", "shared.cw3.tps16.st2", "shared.cw2.tps16.st3"},
-  0};
+  1};
 using SharedSame1P = BaryonFusedSharedWedgeSameOp<double, double2, 4, 2, 1>;
 using SharedSame2P = BaryonFusedSharedWedgeSameOp<double, double2, 4, 2, 2>;
 // General projectors: N'_w = W_w N materialised per site.
