@@ -546,7 +546,9 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   if (job.volume == 0) return cudaSuccess;
   if (tensor_cores && job.prec != Prec::C64) return cudaErrorInvalidValue;
   // job.variant (autotuner): complex64 -- 1 runs the three-kernel form, 2 the
-  // fused kernel with 16 site warps; tensor cores -- the k-steps per work unit
+  // fused kernel with 16 site warps, 0 with 8; tensor cores -- the k-steps per
+  // work unit.  With no variant chosen, two fields take 16 site warps and one
+  // field passed twice 8 (the tuner's choices at 32^3 x 64).
   const bool fused = !tensor_cores && job.prec == Prec::C64 && momentum_fused_supported(plan) && !fused_disabled() &&
                      job.variant != 1;
   const size_t elem = job.prec == Prec::C128 ? sizeof(double2) : sizeof(float2);
@@ -564,7 +566,8 @@ cudaError_t launch_meson_momentum(const Job &job, const OpParams<double> &p, con
   float2 *planes_m = reinterpret_cast<float2 *>(ws + c_bytes);   // mixed form
 
   if (fused) {
-    cudaError_t e = launch_momentum_fused(job, p.in[0], p.in[1], planes_m, plan, job.variant == 2 ? 16 : 8);
+    const bool sw16 = job.variant == 2 || (job.variant < 0 && p.in[0] != p.in[1]);
+    cudaError_t e = launch_momentum_fused(job, p.in[0], p.in[1], planes_m, plan, sw16 ? 16 : 8);
     if (e != cudaSuccess) return e;
     return launch_finalize<float, true>(job, planes_m, static_cast<double2 *>(out), plan);
   }
