@@ -109,7 +109,7 @@ static const VariantSet<float, 7> kFusedCliff2MSame = {
    run_scalar<BaryonFusedCliffMergedOp<float, float2, 4, 16, 2, 2, 0, true>>},
   {"shared_same.cw3.tps8.st2.occ3", "shared_same.cw2.tps8.st2.occ4", "shared_same.cw4.tps8.st2.occ2",
    "shared_same.cw5.tps8.st2.occ2", "same.cw4.tps16.st2.occ3", "same.cw3.tps16.st2.occ4", "same.cw4.tps16.st2"},
-  0};
+  2};
 
 // The shared-wedge forms derive the Gamma_kl^T variant of each type from the
 // Gamma_kl one by the phase ph2[1] - ph2[0], which is the same in every column
