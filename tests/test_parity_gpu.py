@@ -75,6 +75,31 @@ def test_ragged_volumes(api, props, c_oracle):
         assert rel_err(got, c_oracle.meson_two_point(pi, pj, 15, 15)) < TOL_C128, v
 
 
+def test_mixed_ragged_volumes_and_gammas(api, props, c_oracle):
+    """complex64 per-site values through the drop-in functions on ragged volumes
+    and a sweep of gamma selectors (including phased and diagonal ones), against
+    the FP64 oracle relative to the largest value."""
+    from contract_gb300 import pycontract as pc
+    for v in (1, 3, 37, 129, 200):
+        pi, pj, pn = [p[:v] for p in props]
+        got = pc.baryonTwoPoint(cuda(pi, True), cuda(pj, True), cuda(pn, True), 1, 5, 5, 8).cpu().numpy()
+        assert rel_err(got, c_oracle.baryon_two_point(pi, pj, pn, 1, 5, 5, 8)) < 1e-6, v
+        got = pc.mesonTwoPoint(cuda(pi, True), cuda(pj, True), 15, 15).cpu().numpy()
+        assert rel_err(got, c_oracle.meson_two_point(pi, pj, 15, 15)) < 1e-6, v
+    pi, pj, pn = [p[:96] for p in props]
+    a, b, c = cuda(pi, True), cuda(pj, True), cuda(pn, True)
+    for gij, gkl in ((5, 5), (13, 13), (0, 15), (3, 10), (15, 6), (9, 12)):
+        got = pc.mesonTwoPoint(a, b, gij, gkl).cpu().numpy()
+        assert rel_err(got, c_oracle.meson_two_point(pi, pj, gij, gkl)) < 1e-6, (gij, gkl)
+        got = pc.baryonDiquark(a, b, gij, gkl).cpu().numpy().astype(np.complex128)
+        assert rel_err(got, c_oracle.baryon_diquark(pi, pj, gij, gkl)) < 1e-6, (gij, gkl)
+        for t in range(6):
+            for gmn in (0, 8, 15):
+                got = pc.baryonTwoPoint(a, b, c, t, gij, gkl, gmn).cpu().numpy()
+                ref = c_oracle.baryon_two_point(pi, pj, pn, t, gij, gkl, gmn)
+                assert rel_err(got, ref) < 1e-6, (gij, gkl, t, gmn)
+
+
 def test_empty_volume(api):
     import torch
     from contract_gb300 import pycontract as pc
