@@ -98,6 +98,16 @@ def test_mixed_ragged_volumes_and_gammas(api, props, c_oracle):
                 got = pc.baryonTwoPoint(a, b, c, t, gij, gkl, gmn).cpu().numpy()
                 ref = c_oracle.baryon_two_point(pi, pj, pn, t, gij, gkl, gmn)
                 assert rel_err(got, ref) < 1e-6, (gij, gkl, t, gmn)
+    # a dense projector (the materialised-N' triangle and the loop form) for every type
+    rng = np.random.default_rng(29)
+    dense = (rng.standard_normal(16) + 1j * rng.standard_normal(16)) / 4
+    for t in range(6):
+        got = api.baryon(a, b, c, t, 5, 5, project_mn=dense).cpu().numpy()
+        assert rel_err(got, c_oracle.baryon_general_two_point(pi, pj, pn, t, 5, 5, dense)) < 1e-6, t
+    # the all-sink meson (all 16 Gamma_ij at one Gamma_kl), per site
+    for gkl in (5, 10):
+        got = pc.mesonAllSinkTwoPoint(a, b, gkl).cpu().numpy()
+        assert rel_err(got, c_oracle.meson_all_sink(pi, pj, gkl)) < 1e-6, gkl
 
 
 def test_empty_volume(api):
