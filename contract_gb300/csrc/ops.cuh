@@ -132,15 +132,38 @@ __device__ __forceinline__ void build_q_cliff(const BaryonSpin<R> &b, const S *N
   }
 }
 
-// N'_w[m][l] = sum_n W[m][n] N[n][l] into the w-th scratch slot.
+// Largest gamma-basis term count for which build_nprime takes the basis form:
+// ng terms cost ng x 9 complex FMA per N' block, the row form four x 9.
+constexpr int kNprimeCliffTerms = 4;
+
+// N'_w[m][l] = sum_n W[m][n] N[n][l] into the w-th scratch slot.  With
+// `cliff` (b.cl filled for these projectors, few terms) each block is built
+// from the gamma basis instead, N'_w[m][l] = sum_k qc[w][k][m] N[perm[k][m]][l]:
+// cl.ng iterations that every lane takes, where the row form skips W's zero
+// entries per lane and so runs all four n for a warp whose lanes hold
+// different rows m.
 template <class R, class S, int TPS, int NW>
-__device__ __forceinline__ void build_nprime(const BaryonSpin<R> &b, const S *N, S *np, int sub)
+__device__ __forceinline__ void build_nprime(const BaryonSpin<R> &b, const S *N, S *np, int sub, bool cliff = false)
 {
   for (int e = sub; e < 16 * NW; e += TPS) {
     const int w = e / 16, blk = e % 16, m = blk / 4, l = blk % 4;
     const ProjOperand<R> &pw = b.proj[w];
     S *dst = np + (size_t)w * 144 + blk * 9;
-    if (pw.is_perm) {
+    if (cliff) {
+      const CliffordSet<R> &cl = b.cl;
+      cx<R> o[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) o[k] = czero<R>();
+#pragma unroll 1
+      for (int k = 0; k < cl.ng; ++k) {
+        const S *src = N + (cl.perm[k][m] * 4 + l) * 9;
+        const cx<R> c {cl.qc[w][k][m][0], cl.qc[w][k][m][1]};
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cfma(o[q], c, ld<R>(src + q));
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) st(dst + k, o[k]);
+    } else if (pw.is_perm) {
       const S *src = N + (pw.perm[m] * 4 + l) * 9;
 #pragma unroll
       for (int k = 0; k < 9; ++k) st(dst + k, mul_phase(ld<R>(src + k), pw.ph[m]));
@@ -848,7 +871,7 @@ struct BaryonTriOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
-    build_nprime<R, S, TPS, 1>(p.b, in[2], scratch, sub);
+    build_nprime<R, S, TPS, 1>(p.b, in[2], scratch, sub, p.b.cl.ng <= kNprimeCliffTerms);
     __syncwarp();
     triangle_site<R, S, TPS, 1, 1>(p.b, in[0], in[1], scratch, sub, 0, vals);
   }
@@ -960,7 +983,7 @@ struct BaryonFusedOp : OpBase<R, S, CW, TPS, NST> {
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
     S *q = reinterpret_cast<S *>(reinterpret_cast<char *>(scratch) + cbytes<S>(144) * NW);
-    build_nprime<R, S, TPS, NW>(p.b, in[2], scratch, sub);
+    build_nprime<R, S, TPS, NW>(p.b, in[2], scratch, sub, p.b.cl.ng <= kNprimeCliffTerms);
     build_q<R, S, TPS, NW>(p.b, in[2], q, sub);
     __syncwarp();
     cx<R> t[2 * NW];
