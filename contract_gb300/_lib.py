@@ -51,6 +51,7 @@ SIGNATURES = {
     "contract_workspace_reserve": (c_int, [c_size_t]),
     "contract_workspace_bytes": (c_size_t, [c_int_p, c_int]),
     "contract_gamma_table": (None, [c_int_p, c_int_p]),
+    "contract_projector_rank": (c_int, [c_void_p]),
     "contract_convert_precision": (None, [c_void_p, c_void_p, c_size_t, c_int]),
     "contract_convert_layout": (None, [c_void_p, c_void_p, c_int_p, c_int, c_int]),
     "contract_convert_from_quda": (None, [c_void_p, ctypes.POINTER(c_void_p), c_int_p, c_size_t, c_int]),

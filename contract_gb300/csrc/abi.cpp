@@ -538,6 +538,72 @@ void fill_clifford(cgb::CliffordSet<double> &cl, const double *const *projs, int
   }
 }
 
+// A projector W (4x4 complex, row-major) of rank r <= 2 as W = sum_r x_r y_r^T,
+// by elimination with complete pivoting: pivot (p, q) of the remainder E,
+// x_r = E[., q] / E[p][q], y_r = E[p][.], E -= x_r y_r^T.  Taken only when the
+// remainder after at most two steps is exactly zero, so that the factors give W
+// back to rounding; otherwise rk.r stays 0 and the triangle form uses N'.
+void fill_rank(cgb::RankForm<double> &rk, const double *w)
+{
+  rk = {};
+  double e[4][4][2], x[2][4][2] = {}, y[2][4][2] = {};
+  std::memcpy(e, w, sizeof(e));
+  int r = 0;
+  for (;;) {
+    int p = -1, q = -1;
+    double best = 0.0;
+    for (int m = 0; m < 4; ++m)
+      for (int n = 0; n < 4; ++n) {
+        const double a = e[m][n][0] * e[m][n][0] + e[m][n][1] * e[m][n][1];
+        if (a > best) {
+          best = a;
+          p = m;
+          q = n;
+        }
+      }
+    if (p < 0) break;    // the remainder is zero: rank r
+    if (r == 2) return;  // rank > 2
+    const double pr = e[p][q][0], pi = e[p][q][1];
+    for (int m = 0; m < 4; ++m) {  // E[m][q] / E[p][q]
+      x[r][m][0] = (e[m][q][0] * pr + e[m][q][1] * pi) / best;
+      x[r][m][1] = (e[m][q][1] * pr - e[m][q][0] * pi) / best;
+    }
+    x[r][p][0] = 1.0;
+    x[r][p][1] = 0.0;
+    for (int n = 0; n < 4; ++n) {
+      y[r][n][0] = e[p][n][0];
+      y[r][n][1] = e[p][n][1];
+    }
+    for (int m = 0; m < 4; ++m)
+      for (int n = 0; n < 4; ++n) {
+        e[m][n][0] -= x[r][m][0] * y[r][n][0] - x[r][m][1] * y[r][n][1];
+        e[m][n][1] -= x[r][m][0] * y[r][n][1] + x[r][m][1] * y[r][n][0];
+      }
+    for (int k = 0; k < 4; ++k) {  // row p and column q are eliminated
+      e[p][k][0] = e[p][k][1] = 0.0;
+      e[k][q][0] = e[k][q][1] = 0.0;
+    }
+    ++r;
+  }
+  if (r == 0) return;
+  int nnz = 1;
+  for (int side = 0; side < 2; ++side)
+    for (int k = 0; k < r; ++k) {
+      const double(*v)[2] = side ? y[k] : x[k];
+      int c = 0;
+      for (int t = 0; t < 4; ++t)
+        if (v[t][0] != 0.0 || v[t][1] != 0.0) {
+          rk.idx[side][k][c] = (uint8_t)t;
+          rk.c[side][k][c][0] = v[t][0];
+          rk.c[side][k][c][1] = v[t][1];
+          ++c;
+        }
+      nnz = std::max(nnz, c);
+    }
+  rk.r = r;
+  rk.nnz = nnz;
+}
+
 // Contraction type -> canonical form (see ops.cuh): loop or triangle, whether
 // P_i and P_j swap roles, and the c1/c2 phase rows.
 struct TypeForm {
@@ -640,10 +706,13 @@ void do_baryon(void *correl, const void *pi, const void *pj, const void *pn, int
   set_row(p.b.ph2[0], f.c2);
   fill_proj(p.b.proj[0], gmn, proj);
   fill_clifford(p.b.cl, proj ? &proj : nullptr, 1, gmn);
+  if (proj) fill_rank(p.b.rk, proj);
   const cgb::Kind kind = f.loop ? cgb::Kind::BaryonLoop : cgb::Kind::BaryonTri;
   auto run = [&](const cgb::Job &j) { return cgb::launch_baryon(j, f.loop, p); };
-  // aux 0: gamma-basis triangle (one gamma), 1: triangle with N' materialised
-  const cudaError_t e = tuned_launch(kind, job, (f.loop || p.b.cl.ng == 1) ? 0 : 1, run);
+  // aux 0: gamma-basis triangle (one gamma), 1: triangle with N' materialised,
+  // 2: triangle with a projector of rank <= 2
+  const int aux = (f.loop || p.b.cl.ng == 1) ? 0 : (p.b.rk.r > 0 ? 2 : 1);
+  const cudaError_t e = tuned_launch(kind, job, aux, run);
   cuda_ok(e, proj ? "baryon_general_two_point" : "baryon_two_point");
 }
 
@@ -1321,6 +1390,14 @@ int contract_workspace_reserve(size_t bytes)
     return contract_last_error();
   }
   return CONTRACT_SUCCESS;
+}
+
+int contract_projector_rank(const void *project_mn)
+{
+  if (!project_mn) return 0;
+  cgb::RankForm<double> rk;
+  fill_rank(rk, static_cast<const double *>(project_mn));
+  return rk.r;
 }
 
 void contract_gamma_table(int *perm, int *phase)

@@ -76,7 +76,7 @@ int launch_variants(Kind kind, Prec prec, int aux, const char *const **names)
   switch (kind) {
   case Kind::Meson: return meson_variants(prec, names);
   case Kind::BaryonLoop: return baryon_variants(prec, 0, names);
-  case Kind::BaryonTri: return baryon_variants(prec, aux == 0 ? 1 : 2, names);
+  case Kind::BaryonTri: return baryon_variants(prec, aux + 1, names);
   case Kind::BaryonFused: return fused_variants(prec, aux, names);
   case Kind::Diquark: return field_variants(prec, false, names);
   case Kind::Sequential: return field_variants(prec, true, names);

@@ -53,8 +53,8 @@ enum class Kind {
 
 // Number of variants (and their names) for an op at a precision; `aux` is
 // the projector count for BaryonFused and, for BaryonTri, 0 for the
-// gamma-basis form and 1 for the materialised-N' form.  1 means there is
-// nothing to tune.
+// gamma-basis form, 1 for the materialised-N' form and 2 for the form with a
+// projector of rank <= 2.  1 means there is nothing to tune.
 int launch_variants(Kind kind, Prec prec, int aux, const char *const **names);
 
 // Every launcher fills the geometry for its own tile shape and returns the
@@ -133,6 +133,15 @@ template <class R> OpParams<R> convert_params(const OpParams<double> &p)
       }
     }
   }
+  o.b.rk.r = p.b.rk.r;
+  o.b.rk.nnz = p.b.rk.nnz;
+  for (int s = 0; s < 2; ++s)
+    for (int r = 0; r < 2; ++r)
+      for (int k = 0; k < 4; ++k) {
+        o.b.rk.idx[s][r][k] = p.b.rk.idx[s][r][k];
+        o.b.rk.c[s][r][k][0] = R(p.b.rk.c[s][r][k][0]);
+        o.b.rk.c[s][r][k][1] = R(p.b.rk.c[s][r][k][1]);
+      }
   return o;
 }
 

@@ -55,12 +55,23 @@ template <class R> struct CliffordSet {
   R qc[2][16][4][2];  // coef[w][k] * i^ph[k][m]: the coefficient of N[perm[k][m]][m] in Q_w
 };
 
+// A projector of rank r <= 2 as W = sum_r x_r y_r^T (W[m][n] = sum_r x_r[m] y_r[n]).
+// Each vector is a list of nnz (index, coefficient) entries, padded with zero
+// coefficients: [side 0: x_r over rows m, side 1: y_r over columns n][r][k].
+template <class R> struct RankForm {
+  int r;  // 0: the projector is not of this form
+  int nnz;
+  uint8_t idx[2][2][4];
+  R c[2][2][4][2];
+};
+
 template <class R> struct BaryonSpin {
   uint8_t perm1[4], perm2[4];
   uint8_t ph1[2][4];  // [0]: c1 for A = P_i groups, [1]: c1 for the swapped (IM_*) group
   uint8_t ph2[2][4];  // c2 variants (one per output of a loop/tri evaluation)
   ProjOperand<R> proj[2];
   CliffordSet<R> cl;
+  RankForm<R> rk;  // proj[0] factored, for the triangle form
 };
 
 template <class R> struct MesonSpin {
@@ -343,6 +354,65 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
   for (int v = 0; v < NV; ++v)
 #pragma unroll
     for (int w = 0; w < NW; ++w) vals[v * NW + w] = mul_phase(acc[v][w], p1);
+}
+
+// Triangle form with a projector of rank r <= 2 (RankForm).  By bilinearity
+// of the wedge,
+//   sum_m B[j][m] ^ N'[m][l] = sum_r X_r[j] ^ Y_r[l],
+//   X_r[j] = sum_m x_r[m] B[j][m],  Y_r[l] = sum_n y_r[n] N[n][l],
+// so each (i, l) pair takes r wedges and one dot where the N' form takes four
+// wedges.  build_rank writes the 8 r blocks into xy: X_r[j] at block r*4 + j,
+// Y_r[l] at block 8 + r*4 + l.
+template <class R, class S, int TPS>
+__device__ __forceinline__ void build_rank(const RankForm<R> &rk, const S *B, const S *N, S *xy, int sub)
+{
+  const int nb = 4 * rk.r;
+  for (int e = sub; e < 2 * nb; e += TPS) {
+    const int side = e >= nb, rem = e - side * nb, rr = rem / 4, q = rem % 4;
+    // X: B[q][m] at block q*4 + m; Y: N[n][q] at block n*4 + q
+    const S *base = side ? N + q * 9 : B + q * 36;
+    const int stride = side ? 36 : 9;
+    cx<R> o[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) o[k] = czero<R>();
+#pragma unroll 1
+    for (int k = 0; k < rk.nnz; ++k) {
+      const S *src = base + rk.idx[side][rr][k] * stride;
+      const cx<R> c {rk.c[side][rr][k][0], rk.c[side][rr][k][1]};
+#pragma unroll
+      for (int t = 0; t < 9; ++t) cfma(o[t], c, ld<R>(src + t));
+    }
+    S *dst = xy + ((side * 2 + rr) * 4 + q) * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) st(dst + k, o[k]);
+  }
+}
+
+template <class R, class S, int TPS>
+__device__ __forceinline__ cx<R> triangle_rank_site(const BaryonSpin<R> &b, const S *A, const S *xy, int sub)
+{
+  using Ln = Lanes<TPS>;
+  const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT;
+  const int j = b.perm1[i];
+  cx<R> acc = czero<R>();
+#pragma unroll
+  for (int lo = 0; lo < Ln::LPT; ++lo) {
+    const int l = l0 + lo;
+    cx<R> d[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) d[k] = czero<R>();
+#pragma unroll 1
+    for (int rr = 0; rr < b.rk.r; ++rr) {
+      cx<R> x[9], y[9];
+      load9(x, xy + (rr * 4 + j) * 9);
+      load9(y, xy + (8 + rr * 4 + l) * 9);
+      wedge_acc(d, x, y);
+    }
+    cx<R> a[9];
+    load9(a, A + (i * 4 + b.perm2[l]) * 9);
+    acc = cadd(acc, mul_phase(dot9(a, d), b.ph2[0][l]));
+  }
+  return mul_phase(acc, b.ph1[0][i]);
 }
 
 // Triangle form with the projectors in the gamma basis (CliffordSet):
@@ -874,6 +944,20 @@ struct BaryonTriOp : OpBase<R, S, CW, TPS, NST> {
     build_nprime<R, S, TPS, 1>(p.b, in[2], scratch, sub, p.b.cl.ng <= kNprimeCliffTerms);
     __syncwarp();
     triangle_site<R, S, TPS, 1, 1>(p.b, in[0], in[1], scratch, sub, 0, vals);
+  }
+};
+
+// Triangle form, one type per launch, with W of rank <= 2 (e.g. (1 +- g4)/2,
+// rank 2; a polarised projector, rank 1): X_r and Y_r blocks in scratch.
+template <class R, class S, int CW, int TPS, int NST>
+struct BaryonTriRankOp : OpBase<R, S, CW, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 1, EXTRA_BYTES = cbytes<S>(144) + 16;  // +16: bank stagger
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    build_rank<R, S, TPS>(p.b.rk, in[1], in[2], scratch, sub);
+    __syncwarp();
+    vals[0] = triangle_rank_site<R, S, TPS>(p.b, in[0], scratch, sub);
   }
 };
 

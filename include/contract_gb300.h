@@ -99,9 +99,11 @@ int contract_autotune_report(char *buf, size_t n);
  * tune).  op: 0 meson, 1 baryon loop form, 2 baryon triangle form, 3 all
  * types in one pass, 4 diquark, 5 sequential, 6 meson all-source/sink,
  * 7 meson all-gamma momentum projection; precision CONTRACT_C128 or
- * CONTRACT_C64; aux as in the tune-cache keys (the projector count for op 3,
- * +4 when P_i and P_j are one field; for op 7, 2 selects the tensor-core
- * form).  Unknown op or precision: an error, and 0. */
+ * CONTRACT_C64; aux as in the tune-cache keys (for op 2, 0: Gamma_mn one
+ * gamma matrix, 1: N' = W N formed per site, 2: a projector of rank <= 2, see
+ * contract_projector_rank; the projector count for op 3, +4 when P_i and P_j
+ * are one field; for op 7, 2 selects the tensor-core form).  Unknown op or
+ * precision: an error, and 0. */
 int contract_variant_names(int op, int precision, int aux, char *buf, size_t n);
 
 /* Reserve `bytes` of the per-device workspace used by per-timeslice
@@ -114,6 +116,14 @@ size_t contract_workspace_bytes(const int *lattice, int noutputs);
 /* ------------------------------------------------------ gamma algebra -- */
 /* perm[16*4], phase[16*4]: Gamma(n)[r][perm[n*4+r]] = i^phase[n*4+r]. */
 void contract_gamma_table(int *perm, int *phase);
+/* How the per-call triangle kernels apply a projector W (project_mn of
+ * baryon_general_two_point: 16 complex128, row-major W[m][n]): 1 or 2 when W
+ * factors exactly as sum_r x_r y_r^T of that rank, found by elimination with
+ * complete pivoting whose remainder is exactly zero ((1 +- g4)/2: 2; a
+ * polarised projector such as (1 + g4)(1 - i g1 g2)/4: 1), so that each spin
+ * pair takes r colour wedges instead of four; 0 when they form N' = W N per
+ * site instead (rank above 2, W = 0, or project_mn NULL). */
+int contract_projector_rank(const void *project_mn);
 
 /* ------------------------------------------------------- conversion ---- */
 /* complex128 <-> complex64 propagator copy of `volume` sites on the device. */

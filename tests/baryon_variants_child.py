@@ -25,11 +25,14 @@ def main():
     from contract_gb300 import _lib, api
     lib = _lib.lib()
     lib.contract_set_error_mode(1)
-    # [[latt, contract_type, projector: "g4", "pp" or "dense", precision: 1 complex64, 0 complex128], ...]
+    from contract_gb300.pycontract import gamma_matrices
+    # [[latt, contract_type, projector: "g4", "pp", "pol" or "dense", precision: 1 complex64, 0 complex128], ...]
     cases = json.loads(sys.argv[1])
     oracle = L.c_oracle()
     rng = np.random.default_rng(17)
-    projs = {"pp": np.ascontiguousarray(api.projector_plus_minus()[0]),  # (1 + g4)/2: two gamma-basis terms
+    g, e = gamma_matrices(), np.eye(4)
+    projs = {"pp": np.ascontiguousarray(api.projector_plus_minus()[0]),  # (1 + g4)/2: rank 2
+             "pol": np.ascontiguousarray(((e + g[8]) @ (e - 1j * g[3]) / 4).reshape(16)),  # rank 1
              "dense": np.ascontiguousarray((rng.standard_normal(16) + 1j * rng.standard_normal(16)) / 4)}
     errs = []
     for k, (latt, ctype, kind, prec) in enumerate(cases):

@@ -98,6 +98,28 @@ def test_decompose_gamma():
         pc.decompose_gamma((np.eye(4) + g[8]) / 2)
 
 
+def test_projector_rank(lib):
+    """Projectors that the triangle kernels factor as sum_r x_r y_r^T (rank <= 2,
+    elimination with an exactly zero remainder) and those they apply as N' = W N."""
+    from contract_gb300 import pycontract as pc
+    g = pc.gamma_matrices()
+    e = np.eye(4)
+
+    def rank(w):
+        buf = np.ascontiguousarray(np.asarray(w, np.complex128).reshape(16))
+        return lib.contract_projector_rank(buf.ctypes.data)
+
+    assert rank((e + g[8]) / 2) == 2 and rank((e - g[8]) / 2) == 2
+    assert rank((e + g[8]) @ (e - 1j * g[3]) / 4) == 1
+    assert rank((e - g[8]) @ (e + 1j * g[3]) / 4) == 1
+    x, y = np.array([0.5, 0, -1j, 0.25]), np.array([1, 2j, 0, -0.5])
+    assert rank(np.outer(x, y)) == 1
+    assert rank(e) == 0 and rank(g[5]) == 0 and rank(np.zeros((4, 4))) == 0
+    rng = np.random.default_rng(3)
+    assert rank(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))) == 0
+    assert lib.contract_projector_rank(None) == 0
+
+
 def _run(code):
     return subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT,
                           env=dict(os.environ, PYTHONPATH=ROOT))

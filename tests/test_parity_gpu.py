@@ -110,6 +110,30 @@ def test_mixed_ragged_volumes_and_gammas(api, props, c_oracle):
         assert rel_err(got, c_oracle.meson_all_sink(pi, pj, gkl)) < 1e-6, gkl
 
 
+def test_low_rank_projectors(api, props, c_oracle):
+    """Projectors of rank 2 ((1 +- g4)/2) and rank 1 (polarised) through the
+    per-call general two-point, every type, phased and unphased gammas, both
+    precisions, against the FP64 oracle; the triangle types take the factored
+    form (r colour wedges per spin pair)."""
+    from contract_gb300 import _lib
+    from contract_gb300.pycontract import gamma_matrices
+    lib = _lib.lib()
+    g, e = gamma_matrices(), np.eye(4)
+    projs = [(e + g[8]) / 2, (e - g[8]) / 2, (e + g[8]) @ (e - 1j * g[3]) / 4, (e - g[8]) @ (e + 1j * g[3]) / 4]
+    pi, pj, pn = [p[:200] for p in props]
+    dev = {prec: [cuda(p, prec) for p in (pi, pj, pn)] for prec in (False, True)}
+    for w, rank in zip(projs, (2, 2, 1, 1)):
+        w = np.ascontiguousarray(w.reshape(16))
+        assert lib.contract_projector_rank(w.ctypes.data) == rank
+        for gij, gkl in ((5, 5), (13, 10)):
+            for t in range(6):
+                ref = c_oracle.baryon_general_two_point(pi, pj, pn, t, gij, gkl, w)
+                got = api.baryon(*dev[False], t, gij, gkl, project_mn=w).cpu().numpy()
+                assert rel_err(got, ref) < TOL_C128, (rank, gij, gkl, t)
+                got = api.baryon(*dev[True], t, gij, gkl, project_mn=w).cpu().numpy()
+                assert rel_err(got, ref) < 1e-6, (rank, gij, gkl, t)
+
+
 def test_empty_volume(api):
     import torch
     from contract_gb300 import pycontract as pc
@@ -542,8 +566,9 @@ def test_fused_variants_forced(tmp_path):
 def test_baryon_variants_forced(tmp_path):
     """Every compiled tile-shape variant of the per-call baryon two-point, in
     complex64 and complex128 -- loop form; triangle form with a gamma
-    projector; triangle form with N' materialised, for (1 + g4)/2 and for a
-    dense projector -- forced through a tune cache, against the FP64 oracle.
+    projector; triangle form with N' materialised, for a dense projector;
+    triangle form with a projector of rank <= 2, for (1 + g4)/2 and for a
+    polarised projector -- forced through a tune cache, against the FP64 oracle.
     Each case uses its own lattice shape, so that each tune key fixes one
     variant."""
     import ctypes
@@ -557,8 +582,8 @@ def test_baryon_variants_forced(tmp_path):
     cache = tmp_path / "tune.txt"
     lines, cases, names = [], [], []
     for prec in (1, 0):
-        for c, (op, aux, ctype, kind) in enumerate(((1, 0, 0, "g4"), (2, 0, 1, "g4"), (2, 1, 4, "pp"),
-                                                    (2, 1, 3, "dense"))):
+        for c, (op, aux, ctype, kind) in enumerate(((1, 0, 0, "g4"), (2, 0, 1, "g4"), (2, 1, 4, "dense"),
+                                                    (2, 1, 3, "dense"), (2, 2, 4, "pp"), (2, 2, 5, "pol"))):
             buf = ctypes.create_string_buffer(4096)
             n = lib.contract_variant_names(op, prec, aux, buf, len(buf))
             vnames = buf.value.decode().split()
