@@ -1047,7 +1047,8 @@ WORKLOADS = {"meson8": workload_meson8, "momentum32": workload_momentum32, "sequ
              "batch": workload_batch}
 
 
-PROFILE_OPS = ("fused", "fused128", "fusedsame", "tri", "tri128", "trigen", "trigen128", "loop", "loop128", "momentum",
+PROFILE_OPS = ("fused", "fused128", "fusedsame", "tri", "tri128", "trigen", "trigen128", "tridense", "tridense128",
+               "loop", "loop128", "momentum",
                "momentum128", "momentum_tc", "meson", "meson128", "meson_all",
                "diquark", "sequential", "sequential128", "batch_mixed")
 
@@ -1082,6 +1083,8 @@ def run_profile(args):
     prec = 1 if c64 else 0
     latt_c = (ctypes.c_int * 4)(*latt)
     projs = np.ascontiguousarray(api.projector_plus_minus())
+    rng = np.random.default_rng(5)
+    dense = np.ascontiguousarray((rng.standard_normal(16) + 1j * rng.standard_normal(16)) / 4)
     out = torch.empty((16, max(v, 1)), dtype=torch.complex128, device=dev)
     field = torch.empty_like(props[0])
     a, b_, c = (x.data_ptr() for x in props)
@@ -1113,8 +1116,10 @@ def run_profile(args):
             lib.contract_baryon_all_types(out.data_ptr(), a, a, c, v, 5, 5, 2, projs.ctypes.data, prec, latt_c)
         elif base in ("tri", "loop"):  # baryon_two_point form: Gamma_mn = g4
             lib.contract_baryon(out.data_ptr(), a, b_, c, 1 if base == "tri" else 0, v, 5, 5, 8, None, prec, latt_c)
-        elif base == "trigen":  # general projector (1 + g4)/2
+        elif base == "trigen":  # general projector (1 + g4)/2 (rank 2: the factored form)
             lib.contract_baryon(out.data_ptr(), a, b_, c, 1, v, 5, 5, 0, projs[0].ctypes.data, prec, latt_c)
+        elif base == "tridense":  # a dense projector (rank 4: N' = W N per site)
+            lib.contract_baryon(out.data_ptr(), a, b_, c, 1, v, 5, 5, 0, dense.ctypes.data, prec, latt_c)
         elif base == "meson":
             lib.contract_meson(out.data_ptr(), a, b_, v, 15, 15, prec, latt_c)
         elif base == "meson_all":
