@@ -1048,7 +1048,7 @@ WORKLOADS = {"meson8": workload_meson8, "momentum32": workload_momentum32, "sequ
 
 
 PROFILE_OPS = ("fused", "fused128", "fusedsame", "tri", "tri128", "trigen", "trigen128", "tridense", "tridense128",
-               "loop", "loop128", "momentum",
+               "loop", "loop128", "loopgen", "loopgen128", "momentum",
                "momentum128", "momentum_tc", "meson", "meson128", "meson_all",
                "diquark", "sequential", "sequential128", "batch_mixed")
 
@@ -1118,6 +1118,8 @@ def run_profile(args):
             lib.contract_baryon(out.data_ptr(), a, b_, c, 1 if base == "tri" else 0, v, 5, 5, 8, None, prec, latt_c)
         elif base == "trigen":  # general projector (1 + g4)/2 (rank 2: the factored form)
             lib.contract_baryon(out.data_ptr(), a, b_, c, 1, v, 5, 5, 0, projs[0].ctypes.data, prec, latt_c)
+        elif base == "loopgen":  # loop form (type 0) with the general projector (1 + g4)/2
+            lib.contract_baryon(out.data_ptr(), a, b_, c, 0, v, 5, 5, 0, projs[0].ctypes.data, prec, latt_c)
         elif base == "tridense":  # a dense projector (rank 4: N' = W N per site)
             lib.contract_baryon(out.data_ptr(), a, b_, c, 1, v, 5, 5, 0, dense.ctypes.data, prec, latt_c)
         elif base == "meson":

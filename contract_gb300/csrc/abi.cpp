@@ -457,6 +457,10 @@ void fill_proj(cgb::ProjOperand<double> &w, int gamma_mn, const double *project_
   for (int k = 0; k < 16; ++k) {
     w.w[k][0] = project_mn[2 * k];
     w.w[k][1] = project_mn[2 * k + 1];
+    if (w.w[k][0] != 0.0 || w.w[k][1] != 0.0) {
+      w.nzk[w.nnz++] = (uint8_t)k;
+      w.nzmask |= 1u << k;
+    }
   }
   // A phased permutation (one entry in {1, i, -1, -i} per row, distinct
   // columns) is applied with index/sign operations instead of multiplies.

@@ -116,6 +116,9 @@ template <class R> OpParams<R> convert_params(const OpParams<double> &p)
       d.ph[k] = s.ph[k];
     }
     d.is_perm = s.is_perm;
+    d.nnz = s.nnz;
+    d.nzmask = s.nzmask;
+    for (int k = 0; k < 16; ++k) d.nzk[k] = s.nzk[k];
   }
   o.b.cl.ng = p.b.cl.ng;
   for (int k = 0; k < 16; ++k) {
