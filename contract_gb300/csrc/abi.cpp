@@ -552,6 +552,8 @@ void fill_rank(cgb::RankForm<double> &rk, const double *w)
   rk = {};
   double e[4][4][2], x[2][4][2] = {}, y[2][4][2] = {};
   std::memcpy(e, w, sizeof(e));
+  for (int k = 0; k < 32; ++k)
+    if (!std::isfinite(w[k])) return;  // N' carries NaN and Inf through as the reference does
   int r = 0;
   for (;;) {
     int p = -1, q = -1;

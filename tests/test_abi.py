@@ -118,6 +118,9 @@ def test_projector_rank(lib):
     rng = np.random.default_rng(3)
     assert rank(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))) == 0
     assert lib.contract_projector_rank(None) == 0
+    nan = (e + g[8]) / 2
+    nan[3, 0] = np.nan  # a zero entry of the rank-2 projector: the factors would drop it
+    assert rank(nan) == 0
 
 
 def _run(code):
