@@ -1047,7 +1047,7 @@ WORKLOADS = {"meson8": workload_meson8, "momentum32": workload_momentum32, "sequ
              "batch": workload_batch}
 
 
-PROFILE_OPS = ("fused", "fused128", "fusedsame", "tri", "tri128", "trigen", "trigen128", "tridense", "tridense128",
+PROFILE_OPS = ("fused", "fused128", "fused1", "fused1128", "fusedsame", "tri", "tri128", "trigen", "trigen128", "tridense", "tridense128",
                "loop", "loop128", "loopgen", "loopgen128", "momentum",
                "momentum128", "momentum_tc", "meson", "meson128", "meson_all",
                "diquark", "sequential", "sequential128", "batch_mixed")
@@ -1112,6 +1112,8 @@ def run_profile(args):
     def step():
         if base == "fused":
             lib.contract_baryon_all_types(out.data_ptr(), a, b_, c, v, 5, 5, 2, projs.ctypes.data, prec, latt_c)
+        elif base == "fused1":  # one projector, (1 + g4)/2 (rank 2: the factored triangles)
+            lib.contract_baryon_all_types(out.data_ptr(), a, b_, c, v, 5, 5, 1, projs.ctypes.data, prec, latt_c)
         elif base == "fusedsame":  # one field passed as P_i and P_j
             lib.contract_baryon_all_types(out.data_ptr(), a, a, c, v, 5, 5, 2, projs.ctypes.data, prec, latt_c)
         elif base in ("tri", "loop"):  # baryon_two_point form: Gamma_mn = g4

@@ -907,6 +907,7 @@ void fill_all_types(OpParams<double> &p, const void *pi, const void *pj, const v
   const double *pw[2] = {pr, pr + 32};
   for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
   fill_clifford(p.b.cl, pw, nproj, 0);
+  if (nproj == 1) fill_rank(p.b.rk, pw[0]);
 }
 
 cudaError_t run_all_types(const cgb::Job &job, const OpParams<double> &p, int nproj)
@@ -1709,6 +1710,7 @@ int contract_baryon_all_types_noalloc(void *correl, const void *propag_i, const 
   const double *pw[2] = {pr, pr + 32};
   for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
   fill_clifford(p.b.cl, pw, nproj, 0);
+  if (nproj == 1) fill_rank(p.b.rk, pw[0]);
   const cudaError_t e = cgb::launch_baryon_fused(job, nproj, p);
   if (e != cudaSuccess && ws.requested > ws.cap) {
     invalid("lattice {%d, %d, %d, %d} needs %zu bytes of partial sums, more than the %zu-byte static scratch of "

@@ -32,6 +32,9 @@ using Fused1P = BaryonFusedOp<double, double2, 4, 16, 2, 1>;
 using Fused2P = BaryonFusedOp<double, double2, 4, 16, 2, 2>;
 using Fused1M = BaryonFusedOp<float, float2, 8, 16, 2, 1>;
 using Fused2M = BaryonFusedOp<float, float2, 8, 16, 2, 2>;
+// One projector of rank <= 2 that is not one gamma matrix: factored triangles.
+using FusedRank1P = BaryonFusedRankOp<double, double2, 3, 16, 2>;
+using FusedRank1M = BaryonFusedRankOp<float, float2, 4, 16, 2>;
 
 // complex64, FP32-issue bound: consumer warps per SM vs registers per thread.  The
 // shared-wedge variants form each P_i ^ P_j wedge once for both triangle passes;
@@ -125,6 +128,8 @@ template <class R> static bool kl_transpose_is_sign(const OpParams<R> &q)
 cudaError_t launch_baryon_fused(const Job &job, int nw, const OpParams<double> &p)
 {
   const bool cliff = p.b.cl.ng <= nw;
+  if (nw == 1 && !cliff && p.b.rk.r > 0)
+    return job.prec == Prec::C128 ? run_scalar<FusedRank1P>(job, p) : run_scalar<FusedRank1M>(job, convert_params<float>(p));
   if (job.prec == Prec::C128) {
     if (cliff && kl_transpose_is_sign(p)) {
       if (fused_same_ij(p))

@@ -374,24 +374,25 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
 //   sum_m B[j][m] ^ N'[m][l] = sum_r X_r[j] ^ Y_r[l],
 //   X_r[j] = sum_m x_r[m] B[j][m],  Y_r[l] = sum_n y_r[n] N[n][l],
 // so each (i, l) pair takes r wedges and one dot where the N' form takes four
-// wedges.  build_rank writes the 8 r blocks into xy: X_r[j] at block r*4 + j,
-// Y_r[l] at block 8 + r*4 + l.
+// wedges.  build_rank writes X_r[j] (from B) at block r*4 + j of xy, Y_r[l] at
+// block 8 + r*4 + l and, when B2 is given, X_r[j] from B2 at block 16 + r*4 + j.
 template <class R, class S, int TPS>
-__device__ __forceinline__ void build_rank(const RankForm<R> &rk, const S *B, const S *N, S *xy, int sub)
+__device__ __forceinline__ void build_rank(const RankForm<R> &rk, const S *B, const S *N, const S *B2, S *xy,
+                                           int sub)
 {
-  const int nb = 4 * rk.r;
-  for (int e = sub; e < 2 * nb; e += TPS) {
-    const int side = e >= nb, rem = e - side * nb, rr = rem / 4, q = rem % 4;
-    // X: B[q][m] at block q*4 + m; Y: N[n][q] at block n*4 + q
-    const S *base = side ? N + q * 9 : B + q * 36;
-    const int stride = side ? 36 : 9;
+  const int nb = 4 * rk.r, sides = B2 ? 3 : 2;
+  for (int e = sub; e < sides * nb; e += TPS) {
+    const int side = e / nb, rem = e - side * nb, rr = rem / 4, q = rem % 4;
+    const int ycol = side == 1;  // Y: N[n][q] at block n*4 + q; X: B[q][m] at block q*4 + m
+    const S *base = ycol ? N + q * 9 : (side ? B2 : B) + q * 36;
+    const int stride = ycol ? 36 : 9;
     cx<R> o[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) o[k] = czero<R>();
 #pragma unroll 1
     for (int k = 0; k < rk.nnz; ++k) {
-      const S *src = base + rk.idx[side][rr][k] * stride;
-      const cx<R> c {rk.c[side][rr][k][0], rk.c[side][rr][k][1]};
+      const S *src = base + rk.idx[ycol][rr][k] * stride;
+      const cx<R> c {rk.c[ycol][rr][k][0], rk.c[ycol][rr][k][1]};
 #pragma unroll
       for (int t = 0; t < 9; ++t) cfma(o[t], c, ld<R>(src + t));
     }
@@ -401,13 +402,18 @@ __device__ __forceinline__ void build_rank(const RankForm<R> &rk, const S *B, co
   }
 }
 
-template <class R, class S, int TPS>
-__device__ __forceinline__ cx<R> triangle_rank_site(const BaryonSpin<R> &b, const S *A, const S *xy, int sub)
+// Triangle values for the NV c2 variants from X_r (block r*4 + j of X) and
+// Y_r (block r*4 + l of Y); c1 from ph1[c1sel].
+template <class R, class S, int TPS, int NV>
+__device__ __forceinline__ void triangle_rank_site(const BaryonSpin<R> &b, const S *A, const S *X, const S *Y, int sub,
+                                                   int c1sel, cx<R> *vals)
 {
   using Ln = Lanes<TPS>;
   const int i = sub / Ln::TPI, l0 = (sub % Ln::TPI) * Ln::LPT;
   const int j = b.perm1[i];
-  cx<R> acc = czero<R>();
+  cx<R> acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) acc[v] = czero<R>();
 #pragma unroll
   for (int lo = 0; lo < Ln::LPT; ++lo) {
     const int l = l0 + lo;
@@ -417,15 +423,18 @@ __device__ __forceinline__ cx<R> triangle_rank_site(const BaryonSpin<R> &b, cons
 #pragma unroll 1
     for (int rr = 0; rr < b.rk.r; ++rr) {
       cx<R> x[9], y[9];
-      load9(x, xy + (rr * 4 + j) * 9);
-      load9(y, xy + (8 + rr * 4 + l) * 9);
+      load9(x, X + (rr * 4 + j) * 9);
+      load9(y, Y + (rr * 4 + l) * 9);
       wedge_acc(d, x, y);
     }
     cx<R> a[9];
     load9(a, A + (i * 4 + b.perm2[l]) * 9);
-    acc = cadd(acc, mul_phase(dot9(a, d), b.ph2[0][l]));
+    const cx<R> t = dot9(a, d);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) acc[v] = cadd(acc[v], mul_phase(t, b.ph2[v][l]));
   }
-  return mul_phase(acc, b.ph1[0][i]);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) vals[v] = mul_phase(acc[v], b.ph1[c1sel][i]);
 }
 
 // Triangle form with the projectors in the gamma basis (CliffordSet):
@@ -968,9 +977,9 @@ struct BaryonTriRankOp : OpBase<R, S, CW, TPS, NST> {
   static constexpr bool FIELD = false;
   __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
   {
-    build_rank<R, S, TPS>(p.b.rk, in[1], in[2], scratch, sub);
+    build_rank<R, S, TPS>(p.b.rk, in[1], in[2], nullptr, scratch, sub);
     __syncwarp();
-    vals[0] = triangle_rank_site<R, S, TPS>(p.b, in[0], scratch, sub);
+    triangle_rank_site<R, S, TPS, 1>(p.b, in[0], scratch, scratch + 72, sub, 0, vals);
   }
 };
 
@@ -1068,6 +1077,33 @@ struct BaryonFusedSharedWedgeSameOp : OpBase<R, S, CW, 8, NST> {
     build_q_cliff<R, S, 8, NW>(p.b, in[1], scratch, sub);
     __syncwarp();
     fused_shared_wedge_same_site<R, S, NW>(p.b, in[0], in[1], scratch, sub, vals);
+  }
+};
+
+// All six types for one projector of rank <= 2 that is not one gamma matrix
+// (e.g. (1 + g4)/2 alone): the loop types through Q, the triangle types through
+// the factored form, with X_r from P_j for the first triangle pass and from P_i
+// for the swapped one, Y_r from P_n shared by both.  Output o = type.
+template <class R, class S, int CW, int TPS, int NST>
+struct BaryonFusedRankOp : OpBase<R, S, CW, TPS, NST> {
+  static constexpr int NIN = 3, NOUT = 6, EXTRA_BYTES = cbytes<S>(216) + cbytes<S>(9);
+  static constexpr bool FIELD = false;
+  __device__ static void site(const OpParams<R> &p, const S *const *in, S *scratch, int sub, cx<R> *vals)
+  {
+    S *q = scratch + 216;  // after the 24 X, Y, X' blocks
+    build_q<R, S, TPS, 1>(p.b, in[2], q, sub);
+    build_rank<R, S, TPS>(p.b.rk, in[1], in[2], in[0], scratch, sub);
+    __syncwarp();
+    cx<R> t[2];
+    loop_site<R, S, TPS, 2, 1>(p.b, in[0], in[1], q, sub, 0, t);  // IK_JL_NM, IL_JK_NM
+    vals[0] = t[0];
+    vals[2] = t[1];
+    triangle_rank_site<R, S, TPS, 2>(p.b, in[0], scratch, scratch + 72, sub, 0, t);  // IK_JM_NL, IL_JM_NK
+    vals[1] = t[0];
+    vals[3] = t[1];
+    triangle_rank_site<R, S, TPS, 2>(p.b, in[1], scratch + 144, scratch + 72, sub, 1, t);  // IM_JK_NL, IM_JL_NK
+    vals[4] = t[0];
+    vals[5] = t[1];
   }
 };
 

@@ -244,6 +244,33 @@ def test_fused_all_types_one_and_four_term_projectors(api, props, c_oracle):
             assert per_t_rel(got64[t, 0], ref[t, w], ref_site[t, w]) < TOL_C64_TIMESLICE, (t, w)
 
 
+def test_fused_all_types_one_low_rank_projector(api, props, c_oracle):
+    """One projector of rank 2 ((1 +- g4)/2) or rank 1 (polarised) through the
+    fused pass, which takes the factored triangle form for it: per timeslice
+    and per site, two fields and one field for P_i and P_j, phased gammas,
+    both precisions, against the FP64 oracle."""
+    from contract_gb300.pycontract import gamma_matrices
+    pi, pj, pn = props
+    g, e = gamma_matrices(), np.eye(4)
+    for w in ((e + g[8]) / 2, (e - g[8]) / 2, (e + g[8]) @ (e - 1j * g[3]) / 4):
+        w = np.ascontiguousarray(w.reshape(1, 16))
+        for gij, gkl, one_field in ((5, 5, False), (5, 5, True), (13, 10, False)):
+            b = pi if one_field else pj
+            site = np.array([c_oracle.baryon_general_two_point(pi, b, pn, t, gij, gkl, w[0]) for t in range(6)])
+            ref = eo.timeslice_sum(site, LATT)
+            for c64 in (False, True):
+                da, dn = cuda(pi, c64), cuda(pn, c64)
+                db = da if one_field else cuda(pj, c64)
+                got = api.baryon_all_types(da, db, dn, gij, gkl, w, latt=LATT).cpu().numpy()[:, 0]
+                if c64:
+                    for t in range(6):
+                        assert per_t_rel(got[t], ref[t], site[t]) < TOL_C64_TIMESLICE, (gij, gkl, one_field, t)
+                else:
+                    assert rel_err(got, ref) < TOL_C128, (gij, gkl, one_field)
+                    got = api.baryon_all_types(da, db, dn, gij, gkl, w).cpu().numpy()[:, 0]  # per site
+                    assert rel_err(got, site) < TOL_C128, (gij, gkl, one_field)
+
+
 def test_fused_same_field_c128(api, props, c_oracle):
     """complex128 with one pointer for P_i and P_j: the one-pass shared-wedge form
     (and, for Gamma_ij = g5, whose permutation has fixed points, the merged
