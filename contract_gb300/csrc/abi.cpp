@@ -988,8 +988,10 @@ bool baryon_batch_setup(BaryonBatch &bb, const ContractBaryonBatchItem *items, i
   const double *pw[2] = {pr, pr + 32};
   for (int w = 0; w < nproj; ++w) fill_proj(p.b.proj[w], 0, pw[w]);
   fill_clifford(p.b.cl, pw, nproj, 0);
-  if (p.b.cl.ng > nproj)
-    return invalid("batched contractions need projectors spanned by at most nproj gamma matrices (got %d terms)",
+  if (nproj == 1) fill_rank(p.b.rk, pw[0]);
+  if (p.b.cl.ng > nproj && !(nproj == 1 && p.b.rk.r > 0))
+    return invalid("batched contractions need projectors spanned by at most nproj gamma matrices, or one projector "
+                   "of rank <= 2 (got %d terms)",
                    p.b.cl.ng);
   return true;
 }
@@ -1146,7 +1148,8 @@ void run_mixed_batch(const ContractBaryonBatchItem *bitems, int nb, int gamma_ij
     for (int i = 0; i < nm; ++i) same = same && mitems[i].propag_i == mitems[i].propag_j;
     return same;
   }();
-  if (nb > 0) {
+  // one projector of rank <= 2 (not one gamma matrix) runs its one shape
+  if (nb > 0 && !cgb::batch_rank_form(nproj, bb.p)) {
     const bool same = cgb::batch_same_field(bb.p, bb.specs.data(), nb);
     const char *const *names = nullptr;
     const int nv = cgb::batch_variants(same, &names);

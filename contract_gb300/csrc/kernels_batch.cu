@@ -127,10 +127,17 @@ bool batch_same_field(const OpParams<double> &p, const BatchSpec *specs, int n)
   return same && p.b.perm1[0] != 0;
 }
 
+bool batch_rank_form(int nw, const OpParams<double> &p) { return nw == 1 && p.b.cl.ng > 1 && p.b.rk.r > 0; }
+
 cudaError_t launch_baryon_fused_batch(const Job &job, int nw, const OpParams<double> &p, const BatchSpec *specs, int n,
                                       BaryonFinParams *fin)
 {
-  // Gamma-basis projectors only (e.g. (1 +- g4)/2): no per-site N' buffers.
+  // One projector of rank <= 2 that is not one gamma matrix: factored triangles.
+  if (batch_rank_form(nw, p)) {
+    if (job.prec == Prec::C128) return run_batch<BaryonFusedRankOp<double, double2, 3, 16, 2>>(job, p, specs, n, fin);
+    return run_batch<BaryonFusedRankOp<float, float2, 4, 16, 2>>(job, convert_params<float>(p), specs, n, fin);
+  }
+  // Otherwise gamma-basis projectors only (e.g. (1 +- g4)/2): no per-site N' buffers.
   if (p.b.cl.ng > nw) return cudaErrorInvalidValue;
   if (job.prec == Prec::C128) {
     return nw == 1 ? run_batch<BaryonFusedCliffOp<double, double2, 4, 16, 2, 1>>(job, p, specs, n, fin)

@@ -232,7 +232,10 @@ typedef struct {
 /* contract_baryon_all_types (per-timeslice) for up to 128 items in one
  * persistent launch driven by a device work queue, plus one finalisation
  * launch; items is a HOST array.  Projectors must be spanned by at most
- * nproj gamma matrices (e.g. (1 +- g4)/2).  No host synchronisation: after a
+ * nproj gamma matrices (e.g. (1 +- g4)/2 with nproj = 2), or be one projector
+ * of rank <= 2 (contract_projector_rank; e.g. (1 + g4)/2 alone with
+ * nproj = 1, which runs the factored triangle form in both passes and one
+ * tile shape).  No host synchronisation: after a
  * warm-up call (and contract_workspace_reserve) the sequence can be captured
  * in a CUDA graph.  When EVERY item passes one pointer as both propag_i and
  * propag_j, the launch evaluates one triangle pass per site (the second is

@@ -812,6 +812,42 @@ def test_batched_work_queue_and_cuda_graph(api, c64):
 
 
 @pytest.mark.parametrize("c64", [False, True])
+def test_batched_one_low_rank_projector(api, c_oracle, c64):
+    """The batched launch with one projector of rank 2 ((1 + g4)/2 alone: the
+    factored triangle form) over items of different extents, with two fields
+    and with one field for P_i and P_j, against per-item calls and, for the
+    first item, the FP64 oracle."""
+    import torch
+    from contract_gb300 import _lib
+    lib = _lib.lib()
+    w = np.ascontiguousarray(api.projector_plus_minus()[:1])
+    tol = 1e-6 if c64 else 1e-12
+    for one_field in (False, True):
+        items, outs, refs, host = [], [], [], []
+        for k, latt in enumerate(BATCH_LATTS):
+            hp = [eo.make_propagator(latt, 200 + 3 * k + s, 0.1 + 0.1 * s) for s in range(3)]
+            if one_field:
+                hp[1] = hp[0]
+            ps = [cuda(a, c64) for a in hp]
+            if one_field:
+                ps[1] = ps[0]
+            items.append((*ps, latt))
+            host.append(hp)
+            refs.append(api.baryon_all_types(*ps, 5, 5, w, latt=latt).cpu().numpy())
+            outs.append(torch.full((6, 1, latt[3]), float("nan"), dtype=torch.complex128, device="cuda"))
+        arr = _batch_items(items, outs, lib)
+        lib.contract_baryon_all_types_batch(arr, len(outs), 5, 5, 1, w.ctypes.data, 1 if c64 else 0)
+        torch.cuda.synchronize()
+        assert lib.contract_last_error() == 0, lib.contract_last_error_message()
+        for out, ref in zip(outs, refs):
+            assert rel_err(out.cpu().numpy(), ref) < tol, one_field
+        latt = BATCH_LATTS[0]
+        site = np.array([c_oracle.baryon_general_two_point(*host[0], t, 5, 5, w[0]) for t in range(6)])
+        assert rel_err(outs[0].cpu().numpy()[:, 0], eo.timeslice_sum(site, latt)) < (1e-5 if c64 else 1e-12)
+    api.check_device()
+
+
+@pytest.mark.parametrize("c64", [False, True])
 def test_sequential_sink_timeslice(api, props, c_oracle, c64):
     """Sequential source at t_sink: dC/dP on that timeslice, zero elsewhere."""
     import ctypes
