@@ -608,6 +608,37 @@ void fill_rank(cgb::RankForm<double> &rk, const double *w)
     }
   rk.r = r;
   rk.nnz = nnz;
+  // Unit form: within each vector every nonzero entry is the same modulus times
+  // a power of i, and the product of a pair's two moduli is the same for every r.
+  rk.unit = 1;
+  double scale = 0.0;
+  for (int k = 0; k < r && rk.unit; ++k) {
+    double mod[2];
+    for (int side = 0; side < 2 && rk.unit; ++side) {
+      mod[side] = 0.0;
+      for (int t = 0; t < nnz && rk.unit; ++t) {
+        const double a = rk.c[side][k][t][0], b = rk.c[side][k][t][1];
+        if (a == 0.0 && b == 0.0) {  // a padded list: the device adds every entry
+          rk.unit = 0;
+          break;
+        }
+        const double m = std::fabs(a) + std::fabs(b);  // one of a, b is zero for a phase
+        if (mod[side] == 0.0) mod[side] = m;
+        int ph = -1;
+        if (a == m && b == 0.0) ph = 0;
+        else if (a == 0.0 && b == m) ph = 1;
+        else if (a == -m && b == 0.0) ph = 2;
+        else if (a == 0.0 && b == -m) ph = 3;
+        if (ph < 0 || m != mod[side]) rk.unit = 0;
+        else rk.ph[side][k][t] = (uint8_t)ph;
+      }
+    }
+    if (!rk.unit) break;
+    const double s = mod[0] * mod[1];
+    if (k == 0) scale = s;
+    else if (s != scale) rk.unit = 0;
+  }
+  rk.scale = rk.unit ? scale : 1.0;
 }
 
 // Contraction type -> canonical form (see ops.cuh): loop or triangle, whether

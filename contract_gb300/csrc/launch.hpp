@@ -138,10 +138,13 @@ template <class R> OpParams<R> convert_params(const OpParams<double> &p)
   }
   o.b.rk.r = p.b.rk.r;
   o.b.rk.nnz = p.b.rk.nnz;
+  o.b.rk.unit = p.b.rk.unit;
+  o.b.rk.scale = R(p.b.rk.scale);
   for (int s = 0; s < 2; ++s)
     for (int r = 0; r < 2; ++r)
       for (int k = 0; k < 4; ++k) {
         o.b.rk.idx[s][r][k] = p.b.rk.idx[s][r][k];
+        o.b.rk.ph[s][r][k] = p.b.rk.ph[s][r][k];
         o.b.rk.c[s][r][k][0] = R(p.b.rk.c[s][r][k][0]);
         o.b.rk.c[s][r][k][1] = R(p.b.rk.c[s][r][k][1]);
       }

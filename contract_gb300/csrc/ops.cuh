@@ -66,6 +66,13 @@ template <class R> struct RankForm {
   int nnz;
   uint8_t idx[2][2][4];
   R c[2][2][4][2];
+  // unit: every coefficient is scale_v i^ph and scale_x * scale_y is one value
+  // `scale` for every r (true for (1 +- g4)/2 and the polarised projectors):
+  // the complex128 builds then add phased blocks and the triangle values take
+  // `scale` (rank_unit_form).  complex64 keeps the coefficients.
+  int unit;
+  uint8_t ph[2][2][4];
+  R scale;
 };
 
 template <class R> struct BaryonSpin {
@@ -376,6 +383,14 @@ __device__ __forceinline__ void triangle_site(const BaryonSpin<R> &b, const S *A
 // so each (i, l) pair takes r wedges and one dot where the N' form takes four
 // wedges.  build_rank writes X_r[j] (from B) at block r*4 + j of xy, Y_r[l] at
 // block 8 + r*4 + l and, when B2 is given, X_r[j] from B2 at block 16 + r*4 + j.
+// Whether the factored form runs on unit-modulus phases: complex128 only, where
+// the FP64 pipe bounds the kernels (9.81 -> 9.32 ms for (1 + g4)/2 at
+// 24^3 x 64); the complex64 build, on packed FP32 FMAs, measured 2-4 % slower so.
+template <class R> __device__ __forceinline__ bool rank_unit_form(const RankForm<R> &rk)
+{
+  return sizeof(R) == 8 && rk.unit;
+}
+
 template <class R, class S, int TPS>
 __device__ __forceinline__ void build_rank(const RankForm<R> &rk, const S *B, const S *N, const S *B2, S *xy,
                                            int sub)
@@ -389,8 +404,18 @@ __device__ __forceinline__ void build_rank(const RankForm<R> &rk, const S *B, co
     cx<R> o[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) o[k] = czero<R>();
+    const bool unit = rank_unit_form(rk);
+    if (unit) {
 #pragma unroll 1
-    for (int k = 0; k < rk.nnz; ++k) {
+      for (int k = 0; k < rk.nnz; ++k) {
+        const S *src = base + rk.idx[ycol][rr][k] * stride;
+        const uint32_t ph = rk.ph[ycol][rr][k];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) o[t] = cadd(o[t], mul_phase(ld<R>(src + t), ph));
+      }
+    }
+#pragma unroll 1
+    for (int k = 0; k < (unit ? 0 : rk.nnz); ++k) {
       const S *src = base + rk.idx[ycol][rr][k] * stride;
       const cx<R> c {rk.c[ycol][rr][k][0], rk.c[ycol][rr][k][1]};
 #pragma unroll
@@ -433,8 +458,12 @@ __device__ __forceinline__ void triangle_rank_site(const BaryonSpin<R> &b, const
 #pragma unroll
     for (int v = 0; v < NV; ++v) acc[v] = cadd(acc[v], mul_phase(t, b.ph2[v][l]));
   }
+  const R sc = rank_unit_form(b.rk) ? b.rk.scale : R(1);
 #pragma unroll
-  for (int v = 0; v < NV; ++v) vals[v] = mul_phase(acc[v], b.ph1[c1sel][i]);
+  for (int v = 0; v < NV; ++v) {
+    const cx<R> z = mul_phase(acc[v], b.ph1[c1sel][i]);
+    vals[v] = cx<R> {z.x * sc, z.y * sc};
+  }
 }
 
 // Triangle form with the projectors in the gamma basis (CliffordSet):

@@ -119,10 +119,11 @@ def test_low_rank_projectors(api, props, c_oracle):
     from contract_gb300.pycontract import gamma_matrices
     lib = _lib.lib()
     g, e = gamma_matrices(), np.eye(4)
-    projs = [(e + g[8]) / 2, (e - g[8]) / 2, (e + g[8]) @ (e - 1j * g[3]) / 4, (e - g[8]) @ (e + 1j * g[3]) / 4]
+    projs = [(e + g[8]) / 2, (e - g[8]) / 2, (e + g[8]) @ (e - 1j * g[3]) / 4, (e - g[8]) @ (e + 1j * g[3]) / 4,
+             np.outer([0.5, 0, -1j, 0.25], [1, 2j, 0, -0.5])]  # last: factors not all of one modulus
     pi, pj, pn = [p[:200] for p in props]
     dev = {prec: [cuda(p, prec) for p in (pi, pj, pn)] for prec in (False, True)}
-    for w, rank in zip(projs, (2, 2, 1, 1)):
+    for w, rank in zip(projs, (2, 2, 1, 1, 1)):
         w = np.ascontiguousarray(w.reshape(16))
         assert lib.contract_projector_rank(w.ctypes.data) == rank
         for gij, gkl in ((5, 5), (13, 10)):
